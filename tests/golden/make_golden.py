@@ -1,0 +1,109 @@
+"""Generate the golden fixtures that pin the oracle to the reference.
+
+The reference has no tests and no golden outputs, and its stepping path runs
+only on a GPU through cuFFT.  What does run here is its host C code: the
+coefficient setup (sgpstd-qmodeling/funca.c, func.c; sgpstd-qrtm/func.c), the
+windowing helpers and the revolve controller (sgpstd-qrtm/src.c).  ``make -C
+oracle ref`` compiles those files, where they lie, into ``oracle/_ref/``; this
+script calls them on a set of grids and writes their outputs to
+``tests/golden/reference_host.npz`` so the pins also run where the reference
+sources are absent.
+
+Run:  make -C oracle ref && python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", "..", "oracle"))
+import oracle as O  # noqa: E402
+
+fp = C.POINTER(C.c_float)
+ip = C.POINTER(C.c_int)
+
+GRIDS = [  # (pml, fd, nxx, nzz, dx, dz, dt)
+    (20, 20.0, 439, 200, 10.0, 10.0, 0.001),
+    (30, 30.0, 2461, 860, 10.0, 10.0, 0.0005),
+    (10, 30.0, 64, 48, 10.0, 12.5, 0.001),
+    (10, 25.0, 97, 73, 8.0, 10.0, 0.0008),
+]
+REVOLVE = [(10, 3), (100, 5), (2000, 20), (3000, 20), (6000, 40), (5000, 30), (37, 4), (400, 8)]
+
+
+def f32(n):
+    return np.zeros(n, dtype=np.float32)
+
+
+def pf(a):
+    return a.ctypes.data_as(fp)
+
+
+def main():
+    qm_a = O.ref_lib("qm_funca")
+    qm_f = O.ref_lib("qm_func")
+    qr_s = O.ref_lib("qr_src")
+    if qm_a is None or qm_f is None or qr_s is None:
+        raise SystemExit("reference objects missing: run `make -C oracle ref` first")
+    qm_a.get_pml_parameters.argtypes = [C.c_int, C.c_float] + [fp] * 8 + [C.c_int, C.c_int, C.c_float, C.c_float, C.c_float]
+    qm_a.cal_shift_parameters.argtypes = [fp] * 8 + [C.c_float, C.c_float, C.c_int, C.c_int]
+    qm_f.cal_k2d.argtypes = [C.c_float, C.c_float, C.c_int, C.c_int] + [fp] * 4
+    qm_a.rik_cal.argtypes = [C.c_int, C.c_float, C.c_float, fp, C.c_int]
+    qm_a.cal_bbx_bbz.argtypes = [C.c_int, C.c_int, fp, fp, fp]
+    qm_f.transfermodel.argtypes = [C.c_int, C.c_int, C.c_float, C.c_float] + [fp] * 6
+    qr_s.revolve.argtypes = [ip, ip, ip, C.c_int, ip]
+    out = {}
+    for g, (pml, fd, nxx, nzz, dx, dz, dt) in enumerate(GRIDS):
+        pmlt = [f32(nxx), f32(nxx), f32(nzz), f32(nzz), f32(nxx), f32(nxx), f32(nzz), f32(nzz)]
+        qm_a.get_pml_parameters(pml, fd, *[pf(a) for a in pmlt], nxx, nzz, dx, dz, dt)
+        for k, a in zip(["i_ax", "i_bx", "i_az", "i_bz", "h_ax", "h_bx", "h_az", "h_bz"], pmlt):
+            out[f"g{g}_{k}"] = a
+        sh = [f32(nxx), f32(nxx), f32(nzz), f32(nzz), f32(nxx), f32(nxx), f32(nzz), f32(nzz)]
+        # argument order: kxsmr,kxscr,kzsmr,kzscr,kxsmi,kxsci,kzsmi,kzsci
+        names = ["kxsmr", "kxscr", "kzsmr", "kzscr", "kxsmi", "kxsci", "kzsmi", "kzsci"]
+        sh = [f32(nxx if n[1] == "x" else nzz) for n in names]
+        qm_a.cal_shift_parameters(*[pf(a) for a in sh], dx, dz, nxx, nzz)
+        for k, a in zip(names, sh):
+            out[f"g{g}_{k}"] = a
+        if nxx * nzz <= 100000:  # keep the fixture small: 2-D tables for small grids only
+            ks = [f32(nxx * nzz) for _ in range(4)]
+            qm_f.cal_k2d(dx, dz, nxx, nzz, *[pf(a) for a in ks])
+            for k, a in zip(["k2d1", "k2d2", "k2d3", "k2da"], ks):
+                out[f"g{g}_{k}"] = a
+        out[f"g{g}_grid"] = np.array([pml, fd, nxx, nzz, dx, dz, dt], dtype=np.float64)
+    for flag in (1, 2):
+        r = f32(3000)
+        qm_a.rik_cal(3000, 0.0005, 20.0, pf(r), flag)
+        out[f"rik_flag{flag}"] = r
+    rng = np.random.default_rng(7)
+    rho = rng.uniform(1000.0, 2600.0, size=97 * 73).astype(np.float32)
+    bbx, bbz = f32(97 * 73), f32(97 * 73)
+    qm_a.cal_bbx_bbz(97, 73, pf(rho), pf(bbx), pf(bbz))
+    out["bb_rho"], out["bb_bbx"], out["bb_bbz"] = rho, bbx, bbz
+    vp = rng.uniform(1500.0, 4500.0, size=500).astype(np.float32)
+    qp = rng.uniform(20.0, 200.0, size=500).astype(np.float32)
+    tm = [f32(500) for _ in range(4)]
+    qm_f.transfermodel(500, 1, 30.0, 200.0, pf(vp), pf(qp), *[pf(a) for a in tm])
+    out["tm_vp"], out["tm_qp"] = vp, qp
+    for k, a in zip(["gam", "lam", "vwd", "tao"], tm):
+        out[f"tm_{k}"] = a
+    for steps, snaps in REVOLVE:
+        check, capo, fine, info = C.c_int(-1), C.c_int(0), C.c_int(steps), C.c_int(0)
+        tr = []
+        while True:
+            a = qr_s.revolve(C.byref(check), C.byref(capo), C.byref(fine), snaps, C.byref(info))
+            tr.append((a, capo.value, check.value))
+            if a in (5, 6):
+                break
+        out[f"revolve_{steps}_{snaps}"] = np.array(tr, dtype=np.int32)
+    path = os.path.join(HERE, "reference_host.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__":
+    main()
