@@ -1,0 +1,215 @@
+// host_setup.cpp -- one-time FP64 coefficient setup and line-FFT plans.
+//
+// The reference computes its coefficient tables on the host in float
+// (sgpstd-qmodeling/funca.c, func.c); here every table is evaluated in double
+// and rounded once to float.  The formulas are the reference's:
+//   CPML profiles            funca.c:223-340  (get_pml_parameters)
+//   half-cell shift symbols  funca.c:342-432  (cal_shift_parameters)
+//   wavenumbers              funca.c:366-381 / func.c:550-585 (cal_k2d)
+// including the reference's pi = 3.1415926 and its mirror index n/2*2-i for the
+// negative-frequency shift phases.
+#include "host_setup.h"
+
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <vector>
+
+namespace qp {
+
+static const double REF_PI = 3.1415926;  // funca.c:6
+
+void pml_coeffs(int pml, double fm, int nxx, int nzz, double dx, double dz, double dt, std::vector<double>* out8) {
+    const double alpha_max = REF_PI * fm, R = 1e-5, vmax = 5000.0;
+    const int n1 = 2, n2 = 1, n3 = 1;
+    std::vector<double> idx(nxx), idz(nzz), iax(nxx), iaz(nzz), hdx(nxx), hdz(nzz), hax(nxx), haz(nzz);
+    const double dmaxx = (1 + n1 + n2) * vmax * std::log(1.0 / R) / (2.0 * pml * dx);
+    const double dmaxz = (1 + n1 + n2) * vmax * std::log(1.0 / R) / (2.0 * pml * dz);
+    for (int i = 0; i < pml; i++) {
+        const double t1 = std::pow((double)(pml - 1 - i) / pml, n1 + n2);
+        const double t3 = std::pow((double)i / (pml - 1), n3);
+        idx[i] = dmaxx * t1;
+        idz[i] = dmaxz * t1;
+        iax[i] = alpha_max * t3;
+        iaz[i] = iax[i];
+        idx[nxx - 1 - i] = idx[i];
+        idz[nzz - 1 - i] = idz[i];
+        iax[nxx - 1 - i] = iax[i];
+        iaz[nzz - 1 - i] = iaz[i];
+    }
+    for (int i = pml; i < nxx - pml; i++) { idx[i] = 0; iax[i] = iax[pml - 1]; }
+    for (int j = pml; j < nzz - pml; j++) { idz[j] = 0; iaz[j] = iaz[pml - 1]; }
+    for (int i = 0; i < pml - 1; i++) {
+        const double t2 = std::pow((pml - 1.5 - i) / pml, n1 + n2);
+        const double t4 = std::pow((i + 0.5) / (pml - 1), n3);
+        hdx[i] = dmaxx * t2;
+        hdz[i] = dmaxz * t2;
+        hdx[nxx - 2 - i] = hdx[i];
+        hdz[nzz - 2 - i] = hdz[i];
+        hax[i] = alpha_max * t4;
+        haz[i] = hax[i];
+        hax[nxx - 2 - i] = hax[i];
+        haz[nzz - 2 - i] = haz[i];
+    }
+    for (int i = pml - 1; i < nxx - pml; i++) { hdx[i] = 0; hax[i] = hax[pml - 2]; }
+    hdx[nxx - 1] = 0;
+    hax[nxx - 1] = hax[nxx - 2];
+    for (int j = pml - 1; j < nzz - pml; j++) { hdz[j] = 0; haz[j] = haz[pml - 2]; }
+    hdz[nzz - 1] = 0;
+    haz[nzz - 1] = haz[nzz - 2];
+    // order: i_ax, i_bx, i_az, i_bz, h_ax, h_bx, h_az, h_bz
+    for (int k = 0; k < 8; k++) out8[k].assign((k % 4 < 2) ? nxx : nzz, 0.0);
+    for (int i = 0; i < nxx; i++) {
+        double t = idx[i] + iax[i];
+        out8[1][i] = std::exp(-dt * t);
+        out8[0][i] = idx[i] / t * (out8[1][i] - 1.0);
+        t = hdx[i] + hax[i];
+        out8[5][i] = std::exp(-dt * t);
+        out8[4][i] = hdx[i] / t * (out8[5][i] - 1.0);
+    }
+    for (int j = 0; j < nzz; j++) {
+        double t = idz[j] + iaz[j];
+        out8[3][j] = std::exp(-dt * t);
+        out8[2][j] = idz[j] / t * (out8[3][j] - 1.0);
+        t = hdz[j] + haz[j];
+        out8[7][j] = std::exp(-dt * t);
+        out8[6][j] = hdz[j] / t * (out8[7][j] - 1.0);
+    }
+}
+
+double wavenumber(int i, int n, double d) {
+    const double dk = 2.0 * REF_PI / (n * d);
+    return (i < n / 2 + 1) ? i * dk : (n - i) * dk;
+}
+
+// Reference symbol of shift_vxz_kernel / shift_pxz_kernel at index i
+// (acps4.cu:1047-1108): the kernels form H = -b + i a for i < n/2+1 and
+// H = b - i a above, from the table pair (a, b).
+static std::complex<double> ref_symbol(double a, double b, int i, int n) {
+    return (i < n / 2 + 1) ? std::complex<double>(-b, a) : std::complex<double>(b, -a);
+}
+
+void shift_symbols(int n, double d, int which, std::vector<std::complex<double>>& H) {
+    // which: 0 = "m" tables used for the velocity derivative along x
+    //            (kxsmr, kxsmi) ; 1 = "c" tables used for the pressure
+    //            derivative along x (kxscr, kxsci) ; 2 = z velocity derivative
+    //            (kzscr, kzsci) ; 3 = z pressure derivative (kzsmr, kzsmi)
+    std::vector<double> sr(n), si(n), a(n), b(n);
+    const int nh = n / 2 + 1;
+    for (int i = 0; i < n; i++) {
+        if (i < nh) {
+            const double t = i * REF_PI / n;
+            sr[i] = std::cos(t);
+            si[i] = std::sin(t);
+        } else {
+            sr[i] = sr[n / 2 * 2 - i];
+            si[i] = -si[n / 2 * 2 - i];
+        }
+        const double k = wavenumber(i, n, d);
+        switch (which) {
+            case 0: a[i] = k * sr[i]; b[i] = -k * si[i]; break;  // kxsmr, kxsmi
+            case 1: a[i] = k * sr[i]; b[i] = k * si[i]; break;   // kxscr, kxsci
+            case 2: a[i] = k * sr[i]; b[i] = -k * si[i]; break;  // kzscr, kzsci
+            default: a[i] = k * sr[i]; b[i] = k * si[i]; break;  // kzsmr, kzsmi
+        }
+    }
+    // The reference keeps Re of a C2C inverse of real data, i.e. it applies the
+    // Hermitian part (H(k) + conj(H(-k)))/2 of its symbol.  For odd n the
+    // mirrored phases make H itself non-Hermitian, so the effective symbol is
+    // formed explicitly; the 1/n of the line transform is folded in.
+    H.assign(n, 0.0);
+    for (int i = 0; i < n; i++) {
+        const std::complex<double> h = ref_symbol(a[i], b[i], i, n);
+        const int j = (n - i) % n;
+        const std::complex<double> hm = ref_symbol(a[j], b[j], j, n);
+        H[i] = 0.5 * (h + std::conj(hm)) / (double)n;
+    }
+}
+
+// ---- FFT plans --------------------------------------------------------------
+static bool smooth7(int v) {
+    for (int f : {2, 3, 5, 7})
+        while (v % f == 0) v /= f;
+    return v == 1;
+}
+
+static bool factor_direct(int n, std::vector<int>& rad) {
+    rad.clear();
+    int v = n;
+    while (v % 4 == 0) { rad.push_back(4); v /= 4; }
+    while (v % 2 == 0) { rad.push_back(2); v /= 2; }
+    for (int f : {3, 5, 7, 11, 13})
+        while (v % f == 0) { rad.push_back(f); v /= f; }
+    return v == 1 && (int)rad.size() <= QP_MAXST;
+}
+
+// Host Stockham in double (same recurrence as the device engine).
+static void host_fft(std::vector<std::complex<double>>& x, const std::vector<int>& rad, int sgn) {
+    const int n = (int)x.size();
+    std::vector<std::complex<double>> y(n);
+    std::vector<std::complex<double>>*src = &x, *dst = &y;
+    int ns = 1;
+    for (int r : rad) {
+        const int nb = n / r;
+        for (int j = 0; j < nb; j++) {
+            const int k = j % ns;
+            std::complex<double> v[16], o[16];
+            for (int q = 0; q < r; q++) {
+                const double ang = sgn * 2.0 * M_PI * (double)(q * k) / (double)(ns * r);
+                v[q] = (*src)[j + q * nb] * std::complex<double>(std::cos(ang), std::sin(ang));
+            }
+            for (int q = 0; q < r; q++) {
+                std::complex<double> acc = 0;
+                for (int u = 0; u < r; u++) {
+                    const double ang = sgn * 2.0 * M_PI * (double)((u * q) % r) / (double)r;
+                    acc += v[u] * std::complex<double>(std::cos(ang), std::sin(ang));
+                }
+                o[q] = acc;
+            }
+            const int base = (j - k) * r + k;
+            for (int q = 0; q < r; q++) (*dst)[base + q * ns] = o[q];
+        }
+        std::swap(src, dst);
+        ns *= r;
+    }
+    if (src != &x) x = *src;
+}
+
+int build_plan_host(int n, HostPlan& hp) {
+    hp.n = n;
+    hp.blue = 0;
+    if (factor_direct(n, hp.rad)) {
+        hp.m = n;
+    } else {
+        hp.blue = 1;
+        int m = 2 * n - 1;
+        while (!smooth7(m)) m++;
+        hp.m = m;
+        if (!factor_direct(m, hp.rad)) return -1;
+    }
+    const int m = hp.m;
+    hp.w.resize(m);
+    for (int k = 0; k < m; k++) {
+        const double a = -2.0 * M_PI * (double)k / (double)m;
+        hp.w[k] = std::complex<double>(std::cos(a), std::sin(a));
+    }
+    hp.chirp.clear();
+    hp.bhat.clear();
+    if (hp.blue) {
+        hp.chirp.resize(n);
+        for (long long k = 0; k < n; k++) {
+            const long long q = (k * k) % (2LL * n);
+            const double a = -M_PI * (double)q / (double)n;
+            hp.chirp[k] = std::complex<double>(std::cos(a), std::sin(a));
+        }
+        std::vector<std::complex<double>> b(m, 0.0);
+        for (int k = 0; k < n; k++) b[k] = std::conj(hp.chirp[k]);
+        for (int k = 1; k < n; k++) b[m - k] = std::conj(hp.chirp[k]);
+        host_fft(b, hp.rad, -1);
+        hp.bhat.resize(m);
+        for (int k = 0; k < m; k++) hp.bhat[k] = b[k] / (double)m;
+    }
+    return 0;
+}
+
+}  // namespace qp

@@ -1,0 +1,28 @@
+// host_setup.h -- FP64 coefficient setup and line-FFT plan construction.
+#pragma once
+#include <complex>
+#include <vector>
+
+#include "qpstd_internal.h"
+
+namespace qp {
+
+// CPML coefficients; out8 = i_ax, i_bx, i_az, i_bz, h_ax, h_bx, h_az, h_bz.
+void pml_coeffs(int pml, double fm, int nxx, int nzz, double dx, double dz, double dt, std::vector<double>* out8);
+
+// |k| on an n-point grid as the reference builds it (kkx / kkz).
+double wavenumber(int i, int n, double d);
+
+// Effective (Hermitian) staggered-derivative symbol divided by n.
+// which: 0 = x velocity derivative, 1 = x pressure derivative,
+//        2 = z velocity derivative, 3 = z pressure derivative.
+void shift_symbols(int n, double d, int which, std::vector<std::complex<double>>& H);
+
+struct HostPlan {
+    int n = 0, m = 0, blue = 0;
+    std::vector<int> rad;
+    std::vector<std::complex<double>> w, chirp, bhat;
+};
+int build_plan_host(int n, HostPlan& hp);
+
+}  // namespace qp

@@ -1,0 +1,566 @@
+// shot.cu -- per-shot device state, the step schedule and the C ABI.
+//
+// One shot owns one stream, its windowed model and coefficient tables, the
+// source wavefield and (RTM) the receiver wavefield, the revolve checkpoint
+// pool and the image accumulators, all resident in HBM.  The reference's
+// per-shot body of acforward (e.g. sgpstd-qrtm/acsglw.cu:304-1079) maps onto
+// qpstd_shot_create + qpstd_shot_rtm_device + qpstd_shot_get_image.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/qpstd.h"
+#include "host_setup.h"
+#include "qpstd_internal.h"
+#include "revolve.h"
+#include "shot.h"
+
+namespace qp {
+void launch_ac_zpass(const AcZArgs& a, cudaStream_t s);
+void launch_ac_xpass(const AcXArgs& a, cudaStream_t s);
+int ac_set_smem_limits();
+}  // namespace qp
+
+using namespace qp;
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+static int cuda_fail(cudaError_t e, const char* where) {
+    g_err = std::string(where) + ": " + cudaGetErrorString(e);
+    return (e == cudaErrorMemoryAllocation) ? QPSTD_ENOMEM : QPSTD_ECUDA;
+}
+#define CK(call)                                             \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);  \
+    } while (0)
+
+extern "C" const char* qpstd_last_error(void) { return g_err.c_str(); }
+extern "C" int qpstd_version(void) { return 100; }
+
+// ---------------------------------------------------------------------------
+__global__ void add_point_kernel(float* p, float v) { p[0] += v; }
+
+static int upload_plan(qpstd_shot* s, const HostPlan& hp, FFTPlanDev& d) {
+    d.n = hp.n;
+    d.m = hp.m;
+    d.blue = hp.blue;
+    d.nst = (int)hp.rad.size();
+    for (int i = 0; i < d.nst; i++) d.rad[i] = hp.rad[i];
+    const size_t cnt = hp.w.size() + hp.chirp.size() + hp.bhat.size();
+    std::vector<float2> h(cnt);
+    size_t o = 0;
+    for (auto& c : hp.w) h[o++] = make_float2((float)c.real(), (float)c.imag());
+    for (auto& c : hp.chirp) h[o++] = make_float2((float)c.real(), (float)c.imag());
+    for (auto& c : hp.bhat) h[o++] = make_float2((float)c.real(), (float)c.imag());
+    float2* dptr = nullptr;
+    CK(cudaMalloc(&dptr, sizeof(float2) * cnt));
+    s->allocs.push_back(dptr);
+    CK(cudaMemcpy(dptr, h.data(), sizeof(float2) * cnt, cudaMemcpyHostToDevice));
+    d.w = dptr;
+    d.chirp = hp.blue ? dptr + hp.w.size() : nullptr;
+    d.bhat = hp.blue ? dptr + hp.w.size() + hp.chirp.size() : nullptr;
+    return QPSTD_OK;
+}
+
+static int choose_pairs(int nlines, int m) {
+    const int pairs = (nlines + 1) / 2;
+    const int lmax = std::max(1, std::min(8, (96 * 1024) / (16 * m)));
+    int L = (pairs + 2 * 152 - 1) / (2 * 152);
+    return std::max(1, std::min(L, lmax));
+}
+
+static int validate(const qpstd_shot_desc* d) {
+    if (!d) return fail(QPSTD_EINVAL, "null descriptor");
+    if (d->kind < QPSTD_APS || d->kind > QPSTD_QRTM) return fail(QPSTD_EINVAL, "bad kind");
+    if (d->pml < 2 || d->nxx < 2 * d->pml + 1 || d->nzz < 2 * d->pml + 1)
+        return fail(QPSTD_EINVAL, "grid smaller than twice the CPML width");
+    if (d->nt < 1) return fail(QPSTD_EINVAL, "nt < 1");
+    if (!d->vp || !d->rho || !d->bbx || !d->bbz || !d->rik) return fail(QPSTD_EINVAL, "null model pointer");
+    const bool visco = d->kind == QPSTD_VAPS || d->kind == QPSTD_QRTM;
+    if (visco && (!d->gam || !d->lam || !d->vwd || !d->tao)) return fail(QPSTD_EINVAL, "null Q model pointer");
+    if (d->xsg < 0 || d->xsg >= d->nxx || d->zsg < 0 || d->zsg >= d->nzz)
+        return fail(QPSTD_EINVAL, "shot grid index exceeds model");
+    if (d->nr < 0 || (d->nr > 0 && (!d->gxg || !d->gzg))) return fail(QPSTD_EINVAL, "bad receivers");
+    for (int i = 0; i < d->nr; i++)
+        if (d->gxg[i] < 0 || d->gxg[i] >= d->nxx || d->gzg[i] < 0 || d->gzg[i] >= d->nzz)
+            return fail(QPSTD_EINVAL, "receiver grid index exceeds model");
+    const bool rtm = d->kind == QPSTD_ARTM || d->kind == QPSTD_QRTM;
+    if (rtm && (d->snaps < 1 || d->snaps > 64)) return fail(QPSTD_EINVAL, "snaps must be in 1..64");
+    if (d->method != QPSTD_FUSED && d->method != QPSTD_PLAIN) return fail(QPSTD_EINVAL, "bad method");
+    return QPSTD_OK;
+}
+
+static float* dalloc(qpstd_shot* s, size_t n, int* rc) {
+    float* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, sizeof(float) * n);
+    if (e != cudaSuccess) {
+        *rc = cuda_fail(e, "cudaMalloc");
+        return nullptr;
+    }
+    s->allocs.push_back(p);
+    return p;
+}
+
+static int build_receivers(qpstd_shot* s, const qpstd_shot_desc* d) {
+    const int TZ = 2 * s->Lx;
+    s->ntile_x = (s->d.nzz + TZ - 1) / TZ;
+    std::vector<std::vector<RecEntry>> per(s->ntile_x);
+    // winning receiver per cell: the reference marks flagrec/rindex per cell,
+    // the last receiver written wins (acsglw.cu:387-403)
+    std::vector<int> win(d->nr, 1);
+    for (int i = 0; i < d->nr; i++)
+        for (int j = i + 1; j < d->nr; j++)
+            if (d->gxg[i] == d->gxg[j] && d->gzg[i] == d->gzg[j]) { win[i] = 0; break; }
+    for (int i = 0; i < d->nr; i++) {
+        RecEntry e;
+        e.gx = d->gxg[i];
+        e.gz = d->gzg[i];
+        e.ir = i;
+        e.inject = win[i];
+        per[e.gz / TZ].push_back(e);
+    }
+    std::vector<int> off(s->ntile_x + 1, 0);
+    std::vector<RecEntry> flat;
+    for (int t = 0; t < s->ntile_x; t++) {
+        off[t] = (int)flat.size();
+        flat.insert(flat.end(), per[t].begin(), per[t].end());
+    }
+    off[s->ntile_x] = (int)flat.size();
+    int* doff = nullptr;
+    CK(cudaMalloc(&doff, sizeof(int) * off.size()));
+    s->allocs.push_back(doff);
+    CK(cudaMemcpy(doff, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
+    s->rec_off = doff;
+    RecEntry* drec = nullptr;
+    const size_t nrec = std::max<size_t>(flat.size(), 1);
+    CK(cudaMalloc(&drec, sizeof(RecEntry) * nrec));
+    s->allocs.push_back(drec);
+    if (!flat.empty()) CK(cudaMemcpy(drec, flat.data(), sizeof(RecEntry) * flat.size(), cudaMemcpyHostToDevice));
+    s->rec = drec;
+    return QPSTD_OK;
+}
+
+extern "C" int qpstd_shot_create(const qpstd_shot_desc* d, qpstd_shot** out) {
+    if (!out) return fail(QPSTD_EINVAL, "null output handle");
+    *out = nullptr;
+    int rc = validate(d);
+    if (rc) return rc;
+    qpstd_shot* s = new qpstd_shot();
+    s->d = *d;
+    const int nxx = d->nxx, nzz = d->nzz;
+    const size_t N = (size_t)nxx * nzz;
+    s->N = N;
+    s->nx = nxx - 2 * d->pml;
+    s->nz = nzz - 2 * d->pml;
+    s->visco = (d->kind == QPSTD_VAPS || d->kind == QPSTD_QRTM);
+    s->rtm = (d->kind == QPSTD_ARTM || d->kind == QPSTD_QRTM);
+    s->rik.assign(d->rik, d->rik + d->nt);
+    auto bail = [&](int code) {
+        qpstd_shot_destroy(s);
+        return code;
+    };
+    if (s->visco && d->method == QPSTD_FUSED) return bail(fail(QPSTD_ENOTSUP, "fused visco step not built yet"));
+    if (d->method == QPSTD_PLAIN) return bail(fail(QPSTD_ENOTSUP, "plain method not built yet"));
+    static int smem_ok = -1;
+    if (smem_ok != 0) smem_ok = ac_set_smem_limits();
+    cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
+
+    // wavefields: 8 state fields + the pipelined Dx, contiguous
+    s->src.st = dalloc(s, 9 * N, &rc);
+    if (!s->src.st) return bail(rc);
+    if (s->rtm) {
+        s->rcv.st = dalloc(s, 9 * N, &rc);
+        if (!s->rcv.st) return bail(rc);
+    }
+    s->div = dalloc(s, N, &rc);
+    s->Lz = dalloc(s, N, &rc);
+    s->bbx = dalloc(s, N, &rc);
+    s->bbz = dalloc(s, N, &rc);
+    s->c1 = dalloc(s, N, &rc);
+    s->c2 = dalloc(s, N, &rc);
+    if (!s->div || !s->Lz || !s->bbx || !s->bbz || !s->c1 || !s->c2) return bail(rc);
+
+    // models and per-point coefficients (double -> float once)
+    {
+        std::vector<float> c1(N), c2(N);
+        const double dt = d->dt;
+        for (size_t i = 0; i < N; i++) {
+            const double vp = d->vp[i];
+            c1[i] = (float)((double)d->rho[i] * vp * vp * dt);
+            c2[i] = (float)(vp * vp * dt * dt / 12.0);
+        }
+        if ((e = cudaMemcpy(s->c1, c1.data(), 4 * N, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(cuda_fail(e, "upload"));
+        if ((e = cudaMemcpy(s->c2, c2.data(), 4 * N, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(cuda_fail(e, "upload"));
+        if ((e = cudaMemcpy(s->bbx, d->bbx, 4 * N, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(cuda_fail(e, "upload"));
+        if ((e = cudaMemcpy(s->bbz, d->bbz, 4 * N, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(cuda_fail(e, "upload"));
+    }
+    // 1-D tables
+    {
+        std::vector<double> pmlv[8];
+        pml_coeffs(d->pml, d->fd, nxx, nzz, d->dx, d->dz, d->dt, pmlv);
+        const size_t nt1 = 4 * (size_t)nxx + 4 * nzz + nxx + nzz;
+        std::vector<float> h(nt1);
+        size_t o = 0;
+        float* base = dalloc(s, nt1, &rc);
+        if (!base) return bail(rc);
+        const float** dst[8] = {&s->i_ax, &s->i_bx, &s->i_az, &s->i_bz, &s->h_ax, &s->h_bx, &s->h_az, &s->h_bz};
+        for (int k = 0; k < 8; k++) {
+            *dst[k] = base + o;
+            for (double v : pmlv[k]) h[o++] = (float)v;
+        }
+        s->kx2 = base + o;
+        for (int i = 0; i < nxx; i++) {
+            const double k = wavenumber(i, nxx, d->dx);
+            h[o++] = (float)(k * k / nxx);
+        }
+        s->kz2 = base + o;
+        for (int j = 0; j < nzz; j++) {
+            const double k = wavenumber(j, nzz, d->dz);
+            h[o++] = (float)(k * k / nzz);
+        }
+        if ((e = cudaMemcpy(base, h.data(), 4 * nt1, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(cuda_fail(e, "upload"));
+        std::vector<std::complex<double>> H;
+        const size_t nc = 2 * (size_t)nxx + 2 * nzz;
+        std::vector<float2> hc(nc);
+        float2* cbase = nullptr;
+        if ((e = cudaMalloc(&cbase, sizeof(float2) * nc)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc"));
+        s->allocs.push_back(cbase);
+        size_t q = 0;
+        const float2** cdst[4] = {&s->HxM, &s->HxP, &s->HzM, &s->HzP};
+        const int lens[4] = {nxx, nxx, nzz, nzz};
+        const double sp[4] = {d->dx, d->dx, d->dz, d->dz};
+        for (int w = 0; w < 4; w++) {
+            shift_symbols(lens[w], sp[w], w, H);
+            *cdst[w] = cbase + q;
+            for (auto& c : H) hc[q++] = make_float2((float)c.real(), (float)c.imag());
+        }
+        if ((e = cudaMemcpy(cbase, hc.data(), sizeof(float2) * nc, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(cuda_fail(e, "upload"));
+    }
+    // FFT plans and tile shapes
+    {
+        HostPlan hx, hz;
+        if (build_plan_host(nxx, hx) || build_plan_host(nzz, hz)) return bail(fail(QPSTD_ENOTSUP, "no FFT plan for this length"));
+        if ((rc = upload_plan(s, hx, s->px))) return bail(rc);
+        if ((rc = upload_plan(s, hz, s->pz))) return bail(rc);
+        s->Lx = choose_pairs(nzz, s->px.m);
+        s->Lzp = choose_pairs(nxx, s->pz.m);
+        if (16.0 * s->px.m > 200 * 1024 || 16.0 * s->pz.m > 200 * 1024)
+            return bail(fail(QPSTD_ENOTSUP, "line too long for one CTA"));
+    }
+    if ((rc = build_receivers(s, d))) return bail(rc);
+    s->gather = dalloc(s, (size_t)d->nt * std::max(d->nr, 1), &rc);
+    if (!s->gather) return bail(rc);
+    if (s->rtm) {
+        s->store = dalloc(s, (size_t)d->snaps * 8 * N, &rc);
+        s->obs = dalloc(s, (size_t)d->nt * std::max(d->nr, 1), &rc);
+        s->img = dalloc(s, 4 * (size_t)s->nx * s->nz, &rc);
+        if (!s->store || !s->obs || !s->img) return bail(rc);
+        s->img_c = s->img + (size_t)s->nx * s->nz;
+        s->ssg = s->img_c + (size_t)s->nx * s->nz;
+        s->ssg_c = s->ssg + (size_t)s->nx * s->nz;
+    }
+    if ((e = cudaMemset(s->src.st, 0, sizeof(float) * 9 * N)) != cudaSuccess) return bail(cuda_fail(e, "memset"));
+    *out = s;
+    return QPSTD_OK;
+}
+
+extern "C" int qpstd_shot_destroy(qpstd_shot* s) {
+    if (!s) return QPSTD_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (void* p : s->allocs) cudaFree(p);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return QPSTD_OK;
+}
+
+extern "C" int qpstd_shot_set_state(qpstd_shot* s, const float* state) {
+    if (!s || !state) return fail(QPSTD_EINVAL, "null argument");
+    CK(cudaMemcpyAsync(s->src.st, state, sizeof(float) * 8 * s->N, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return QPSTD_OK;
+}
+
+extern "C" int qpstd_shot_get_state(qpstd_shot* s, float* state) {
+    if (!s || !state) return fail(QPSTD_EINVAL, "null argument");
+    CK(cudaMemcpyAsync(state, s->src.st, sizeof(float) * 8 * s->N, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return QPSTD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// acoustic passes
+static AcZArgs zargs(qpstd_shot* s, Wave& w, int do_v, int do_div) {
+    AcZArgs a;
+    a.nxx = s->d.nxx;
+    a.nzz = s->d.nzz;
+    a.L = s->Lzp;
+    a.pl = s->pz;
+    a.HzP = s->HzP;
+    a.HzM = s->HzM;
+    a.kz2 = s->kz2;
+    a.h_az = s->h_az;
+    a.h_bz = s->h_bz;
+    a.i_az = s->i_az;
+    a.i_bz = s->i_bz;
+    a.bbz = s->bbz;
+    a.p = w.p(s->N);
+    a.vz = w.vz(s->N);
+    a.psi_pz = w.fipz(s->N);
+    a.psi_vz = w.fivzz(s->N);
+    a.Dx = w.Dx(s->N);
+    a.div = s->div;
+    a.Lz = s->Lz;
+    a.dt = s->d.dt;
+    a.do_v = do_v;
+    a.do_div = do_div;
+    return a;
+}
+
+static AcXArgs xargs(qpstd_shot* s, Wave& w, int do_p, int do_v, int do_dx) {
+    AcXArgs a;
+    memset(&a, 0, sizeof(a));
+    a.nxx = s->d.nxx;
+    a.nzz = s->d.nzz;
+    a.L = s->Lx;
+    a.pml = s->d.pml;
+    a.pl = s->px;
+    a.HxP = s->HxP;
+    a.HxM = s->HxM;
+    a.kx2 = s->kx2;
+    a.h_ax = s->h_ax;
+    a.h_bx = s->h_bx;
+    a.i_ax = s->i_ax;
+    a.i_bx = s->i_bx;
+    a.bbx = s->bbx;
+    a.c1 = s->c1;
+    a.c2 = s->c2;
+    a.p = w.p(s->N);
+    a.vx = w.vx(s->N);
+    a.psi_px = w.fipx(s->N);
+    a.psi_vx = w.fivxx(s->N);
+    a.Dx = w.Dx(s->N);
+    a.div = s->div;
+    a.Lz = s->Lz;
+    a.dt = s->d.dt;
+    a.do_p = do_p;
+    a.do_v = do_v;
+    a.do_dx = do_dx;
+    a.xs = -1;
+    a.zs = -1;
+    return a;
+}
+
+// Advance the source wavefield over steps t0 .. t0+n-1 (source wavelet index t).
+// gather: device rows for each step (row t-t0), or null.  ssg_on: accumulate
+// the illumination (first sweep of RTM, addsa_kernel restart==0).
+static int advance_src(qpstd_shot* s, int t0, int n, float* gather, bool ssg_on) {
+    if (n <= 0) return QPSTD_OK;
+    Wave& w = s->src;
+    cudaStream_t st = s->stream;
+    launch_ac_xpass(xargs(s, w, 0, 0, 1), st);
+    s->launches++;
+    for (int t = t0; t < t0 + n; t++) {
+        launch_ac_zpass(zargs(s, w, t > t0, 1), st);
+        AcXArgs x = xargs(s, w, 1, 1, t < t0 + n - 1);
+        x.xs = s->d.xsg;
+        x.zs = s->d.zsg;
+        x.src = (t < s->d.nt) ? (float)((double)s->rik[t] * s->d.dt * 1000.0) : 0.f;
+        x.rec_off = s->rec_off;
+        x.rec = s->rec;
+        x.gather_row = gather ? gather + (size_t)(t - t0) * s->d.nr : nullptr;
+        if (ssg_on) {
+            x.ssg = s->ssg;
+            x.ssg_c = s->ssg_c;
+        }
+        launch_ac_xpass(x, st);
+        s->launches += 2;
+    }
+    launch_ac_zpass(zargs(s, w, 1, 0), st);
+    s->launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    return QPSTD_OK;
+}
+
+// One receiver-side step (firsturn / youturn): injected at the receivers from
+// obs row `row`, then imaged against the source wavefield.  The receiver
+// wavefield stays pipelined between calls (its vz update is folded into the
+// next call's z pass); nothing else reads it.
+static int receiver_step(qpstd_shot* s, int row, bool first) {
+    Wave& w = s->rcv;
+    cudaStream_t st = s->stream;
+    launch_ac_zpass(zargs(s, w, first ? 0 : 1, 1), st);
+    AcXArgs x = xargs(s, w, 1, 1, 1);
+    x.rec_off = s->rec_off;
+    x.rec = s->rec;
+    x.obs_row = s->obs + (size_t)row * s->d.nr;
+    x.img = s->img;
+    x.img_c = s->img_c;
+    x.ps = s->src.p(s->N);
+    launch_ac_xpass(x, st);
+    s->launches += 2;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    return QPSTD_OK;
+}
+
+extern "C" int qpstd_shot_advance_device(qpstd_shot* s, int t0, int nsteps) {
+    if (!s || nsteps < 0 || nsteps > s->d.nt || t0 < 0) return fail(QPSTD_EINVAL, "bad advance arguments");
+    s->launches = 0;
+    return advance_src(s, t0, nsteps, s->d.nr > 0 ? s->gather : nullptr, false);
+}
+
+extern "C" int qpstd_shot_advance(qpstd_shot* s, int t0, int nsteps, float* gather) {
+    int rc = qpstd_shot_advance_device(s, t0, nsteps);
+    if (rc) return rc;
+    if (gather && s->d.nr > 0)
+        CK(cudaMemcpyAsync(gather, s->gather, sizeof(float) * (size_t)nsteps * s->d.nr, cudaMemcpyDeviceToHost,
+                           s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return QPSTD_OK;
+}
+
+extern "C" long long qpstd_shot_launch_count(const qpstd_shot* s) { return s ? s->launches : -1; }
+extern "C" long long qpstd_shot_forward_steps(const qpstd_shot* s) { return s ? s->fwd_steps : -1; }
+extern "C" int qpstd_shot_sync(qpstd_shot* s) {
+    if (!s) return fail(QPSTD_EINVAL, "null shot");
+    CK(cudaStreamSynchronize(s->stream));
+    return QPSTD_OK;
+}
+
+extern "C" int qpstd_shot_set_obs(qpstd_shot* s, const float* obs) {
+    if (!s || !obs || !s->rtm) return fail(QPSTD_EINVAL, "set_obs needs an RTM shot and data");
+    if (s->d.nr > 0)
+        CK(cudaMemcpyAsync(s->obs, obs, sizeof(float) * (size_t)s->d.nt * s->d.nr, cudaMemcpyHostToDevice,
+                           s->stream));
+    return QPSTD_OK;
+}
+
+// Revolve-driven RTM, the action loop of sgpstd-qrtm/acps4.cu:449-905 and
+// sgpstd-qrtm/acsglw.cu:470-1039.
+extern "C" int qpstd_shot_rtm_device(qpstd_shot* s) {
+    if (!s || !s->rtm) return fail(QPSTD_EINVAL, "not an RTM shot");
+    const size_t N = s->N, NI = (size_t)s->nx * s->nz;
+    cudaStream_t st = s->stream;
+    s->launches = 0;
+    s->fwd_steps = 0;
+    CK(cudaMemsetAsync(s->src.st, 0, sizeof(float) * 9 * N, st));
+    CK(cudaMemsetAsync(s->rcv.st, 0, sizeof(float) * 9 * N, st));
+    CK(cudaMemsetAsync(s->img, 0, sizeof(float) * 4 * NI, st));
+    Revolve rv(s->d.nt, s->d.snaps);
+    int ts = 0, rc;
+    bool first_sweep = true, first_rcv = true;
+    for (;;) {
+        const RevolveAction act = rv.next();
+        if (act == RV_TAKESHOT) {
+            float* slot = s->store + (size_t)rv.check() * 8 * N;
+            CK(cudaMemcpyAsync(slot, s->src.st, sizeof(float) * 8 * N, cudaMemcpyDeviceToDevice, st));
+            if (rv.capo() == 0) {
+                // checkpoint 0 also holds the first source sample (acsglw.cu:493-500)
+                add_point_kernel<<<1, 1, 0, st>>>(slot + (size_t)s->d.xsg * s->d.nzz + s->d.zsg,
+                                                  (float)((double)s->rik[0] * 1000.0 * s->d.dt));
+                s->launches++;
+            }
+        } else if (act == RV_ADVANCE) {
+            const int n = rv.capo() - ts + 1;
+            if ((rc = advance_src(s, ts, n, nullptr, first_sweep))) return rc;
+            s->fwd_steps += n;
+            ts = rv.capo() + 1;
+        } else if (act == RV_FIRSTURN || act == RV_YOUTURN) {
+            if (act == RV_FIRSTURN) first_sweep = false;
+            const int row = (act == RV_FIRSTURN) ? s->d.nt - 1 : rv.capo();
+            if ((rc = receiver_step(s, row, first_rcv))) return rc;
+            first_rcv = false;
+        } else if (act == RV_RESTORE) {
+            const float* slot = s->store + (size_t)rv.check() * 8 * N;
+            CK(cudaMemcpyAsync(s->src.st, slot, sizeof(float) * 8 * N, cudaMemcpyDeviceToDevice, st));
+            ts = rv.capo() + 1;
+        } else if (act == RV_TERMINATE) {
+            break;
+        } else {
+            char buf[96];
+            snprintf(buf, sizeof(buf), "irregular termination of revolve (info %d)", rv.info());
+            return fail(QPSTD_EREVOLVE, buf);
+        }
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    return QPSTD_OK;
+}
+
+extern "C" int qpstd_shot_get_image(qpstd_shot* s, float* img, float* ssg) {
+    if (!s || !s->rtm) return fail(QPSTD_EINVAL, "not an RTM shot");
+    const size_t NI = (size_t)s->nx * s->nz;
+    if (img) CK(cudaMemcpyAsync(img, s->img, sizeof(float) * NI, cudaMemcpyDeviceToHost, s->stream));
+    if (ssg) CK(cudaMemcpyAsync(ssg, s->ssg, sizeof(float) * NI, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return QPSTD_OK;
+}
+
+// ---------------------------------------------------------------------------
+extern "C" int qpstd_model_shot(const qpstd_shot_desc* d, float* gather, float* state) {
+    if (!d) return fail(QPSTD_EINVAL, "null descriptor");
+    if (d->kind != QPSTD_APS && d->kind != QPSTD_VAPS) return fail(QPSTD_EINVAL, "modeling needs APS or VAPS");
+    qpstd_shot* s = nullptr;
+    int rc = qpstd_shot_create(d, &s);
+    if (rc) return rc;
+    rc = qpstd_shot_advance(s, 0, d->nt, gather);
+    if (!rc && state) rc = qpstd_shot_get_state(s, state);
+    qpstd_shot_destroy(s);
+    return rc;
+}
+
+extern "C" int qpstd_rtm_shot(const qpstd_shot_desc* d, const float* obs, float* img, float* ssg) {
+    if (!d || !obs) return fail(QPSTD_EINVAL, "null argument");
+    if (d->kind != QPSTD_ARTM && d->kind != QPSTD_QRTM) return fail(QPSTD_EINVAL, "RTM needs ARTM or QRTM");
+    qpstd_shot* s = nullptr;
+    int rc = qpstd_shot_create(d, &s);
+    if (rc) return rc;
+    if (!(rc = qpstd_shot_set_obs(s, obs)))
+        if (!(rc = qpstd_shot_rtm_device(s))) rc = qpstd_shot_get_image(s, img, ssg);
+    qpstd_shot_destroy(s);
+    return rc;
+}
+
+// ---------------------------------------------------------------------------
+// 5-point Laplacian filter (filter_image, sgpstd-qrtm/acsglw.cu:1872-1893),
+// bounds-checked so no write leaves the nx*nz image.
+__global__ void filter_image_kernel(int nx, int nz, float rdx2, float rdz2, const float* __restrict__ img,
+                                    float* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nx * nz) return;
+    const int ix = i / nz, iz = i - ix * nz;
+    if (ix == 0 || iz == 0 || ix == nx - 1 || iz == nz - 1) {
+        out[i] = 0.f;
+        return;
+    }
+    out[i] = (img[i + 1] + img[i - 1] - 2.f * img[i]) * rdz2 + (img[i + nz] + img[i - nz] - 2.f * img[i]) * rdx2;
+}
+
+extern "C" int qpstd_filter_image(int nx, int nz, float dx, float dz, const float* img, float* imgf) {
+    if (nx < 1 || nz < 1 || !img || !imgf) return fail(QPSTD_EINVAL, "bad filter arguments");
+    const size_t n = (size_t)nx * nz;
+    float *a = nullptr, *b = nullptr;
+    CK(cudaMalloc(&a, 8 * n));
+    b = a + n;
+    cudaError_t e = cudaMemcpy(a, img, 4 * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        filter_image_kernel<<<(unsigned)((n + 255) / 256), 256>>>(nx, nz, 1.f / (dx * dx), 1.f / (dz * dz), a, b);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(imgf, b, 4 * n, cudaMemcpyDeviceToHost);
+    cudaFree(a);
+    if (e != cudaSuccess) return cuda_fail(e, "filter_image");
+    return QPSTD_OK;
+}

@@ -1,0 +1,55 @@
+// shot.h -- the device-resident state of one shot.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "../../include/qpstd.h"
+#include "qpstd_internal.h"
+
+namespace qp {
+
+// One wavefield: 8 state fields (the reference's checkpoint set, in the order
+// p, vx, vz, fipx, fipz, fivxx, fivzz, aux; storecheckpoints,
+// sgpstd-qrtm/acsglw.cu:1946) followed by Dx, the x part of the next step's
+// divergence that the fused schedule carries between passes.
+struct Wave {
+    float* st = nullptr;
+    float* p(size_t N) { return st; }
+    float* vx(size_t N) { return st + N; }
+    float* vz(size_t N) { return st + 2 * N; }
+    float* fipx(size_t N) { return st + 3 * N; }
+    float* fipz(size_t N) { return st + 4 * N; }
+    float* fivxx(size_t N) { return st + 5 * N; }
+    float* fivzz(size_t N) { return st + 6 * N; }
+    float* aux(size_t N) { return st + 7 * N; }
+    float* Dx(size_t N) { return st + 8 * N; }
+};
+
+}  // namespace qp
+
+struct qpstd_shot {
+    qpstd_shot_desc d{};
+    size_t N = 0;
+    int nx = 0, nz = 0;
+    bool visco = false, rtm = false;
+    cudaStream_t stream = nullptr;
+    std::vector<void*> allocs;
+    qp::Wave src, rcv;
+    float *div = nullptr, *Lz = nullptr;
+    float *bbx = nullptr, *bbz = nullptr, *c1 = nullptr, *c2 = nullptr;
+    const float *i_ax = nullptr, *i_bx = nullptr, *i_az = nullptr, *i_bz = nullptr;
+    const float *h_ax = nullptr, *h_bx = nullptr, *h_az = nullptr, *h_bz = nullptr;
+    const float *kx2 = nullptr, *kz2 = nullptr;
+    const float2 *HxM = nullptr, *HxP = nullptr, *HzM = nullptr, *HzP = nullptr;
+    qp::FFTPlanDev px{}, pz{};
+    int Lx = 1, Lzp = 1, ntile_x = 0;
+    int* rec_off = nullptr;
+    qp::RecEntry* rec = nullptr;
+    std::vector<float> rik;
+    float* gather = nullptr;
+    float* store = nullptr;
+    float* obs = nullptr;
+    float *img = nullptr, *img_c = nullptr, *ssg = nullptr, *ssg_c = nullptr;
+    long long launches = 0, fwd_steps = 0;
+};

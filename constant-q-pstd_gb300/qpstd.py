@@ -1,0 +1,209 @@
+"""Python front end of libqpstd (the GB300 Constant-Q-PSTD hot path).
+
+ctypes bindings of ``include/qpstd.h`` plus numpy helpers.  The CUDA library is
+the only implementation: if ``libqpstd.so`` is missing or cannot be loaded,
+every call raises -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libqpstd.so")
+
+APS, VAPS, ARTM, QRTM = 0, 1, 2, 3
+FUSED, PLAIN = 0, 1
+
+_fp = C.POINTER(C.c_float)
+_ip = C.POINTER(C.c_int)
+
+
+class ShotDesc(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int), ("method", C.c_int),
+        ("nxx", C.c_int), ("nzz", C.c_int), ("pml", C.c_int),
+        ("dx", C.c_float), ("dz", C.c_float), ("dt", C.c_float), ("fd", C.c_float),
+        ("nt", C.c_int),
+        ("vp", _fp), ("rho", _fp), ("bbx", _fp), ("bbz", _fp),
+        ("gam", _fp), ("lam", _fp), ("vwd", _fp), ("tao", _fp),
+        ("rik", _fp), ("xsg", C.c_int), ("zsg", C.c_int),
+        ("nr", C.c_int), ("gxg", _ip), ("gzg", _ip),
+        ("etas", C.c_float), ("etar", C.c_float), ("taoc", C.c_float),
+        ("snaps", C.c_int),
+    ]
+
+
+class QpstdError(RuntimeError):
+    pass
+
+
+def build(verbose: bool = False) -> None:
+    """Compile libqpstd.so in-tree for sm_103a (nvcc; no GPU needed)."""
+    jobs = str(min(8, os.cpu_count() or 1))
+    out = None if verbose else subprocess.DEVNULL
+    subprocess.run(["make", "-s", "-j", jobs, "-C", HERE], check=True, stdout=out)
+
+
+_lib = None
+
+EXPORTS = {
+    "qpstd_last_error": (C.c_char_p, []),
+    "qpstd_version": (C.c_int, []),
+    "qpstd_model_shot": (C.c_int, [C.POINTER(ShotDesc), _fp, _fp]),
+    "qpstd_rtm_shot": (C.c_int, [C.POINTER(ShotDesc), _fp, _fp, _fp]),
+    "qpstd_filter_image": (C.c_int, [C.c_int, C.c_int, C.c_float, C.c_float, _fp, _fp]),
+    "qpstd_shot_create": (C.c_int, [C.POINTER(ShotDesc), C.POINTER(C.c_void_p)]),
+    "qpstd_shot_destroy": (C.c_int, [C.c_void_p]),
+    "qpstd_shot_set_state": (C.c_int, [C.c_void_p, _fp]),
+    "qpstd_shot_get_state": (C.c_int, [C.c_void_p, _fp]),
+    "qpstd_shot_advance": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _fp]),
+    "qpstd_shot_advance_device": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "qpstd_shot_launch_count": (C.c_longlong, [C.c_void_p]),
+    "qpstd_shot_set_obs": (C.c_int, [C.c_void_p, _fp]),
+    "qpstd_shot_rtm_device": (C.c_int, [C.c_void_p]),
+    "qpstd_shot_get_image": (C.c_int, [C.c_void_p, _fp, _fp]),
+    "qpstd_shot_forward_steps": (C.c_longlong, [C.c_void_p]),
+    "qpstd_shot_sync": (C.c_int, [C.c_void_p]),
+}
+
+
+def lib():
+    """Load libqpstd.so (raises if it is absent: the CUDA path is mandatory)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise QpstdError(f"{LIB_PATH} not built; run build() (the CUDA library has no fallback)")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in EXPORTS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise QpstdError(f"libqpstd error {rc}: {lib().qpstd_last_error().decode()}")
+
+
+def _f(a):
+    return a.ctypes.data_as(_fp) if a is not None else None
+
+
+class Desc:
+    """Owns the float32/int32 arrays a qpstd_shot_desc points at."""
+
+    def __init__(self, d: dict, method: int = FUSED):
+        self.keep = {}
+        s = ShotDesc()
+        s.kind = int(d["kind"])
+        s.method = int(d.get("method", method))
+        for k in ("nxx", "nzz", "pml", "nt", "xsg", "zsg", "snaps"):
+            setattr(s, k, int(d.get(k, 0)))
+        for k in ("dx", "dz", "dt", "fd", "etas", "etar", "taoc"):
+            setattr(s, k, float(d.get(k, 0.0)))
+        for k in ("vp", "rho", "bbx", "bbz", "gam", "lam", "vwd", "tao", "rik"):
+            if d.get(k) is not None:
+                a = np.ascontiguousarray(d[k], dtype=np.float32).ravel()
+                self.keep[k] = a
+                setattr(s, k, _f(a))
+        gx = np.ascontiguousarray(d["gxg"], dtype=np.int32)
+        gz = np.ascontiguousarray(d["gzg"], dtype=np.int32)
+        self.keep["gx"], self.keep["gz"] = gx, gz
+        s.nr = gx.size
+        s.gxg = gx.ctypes.data_as(_ip)
+        s.gzg = gz.ctypes.data_as(_ip)
+        self.s = s
+        self.d = d
+
+
+def model_shot(d: dict, method: int = FUSED, want_state: bool = False):
+    D = Desc(d, method)
+    g = np.zeros((d["nt"], D.s.nr), dtype=np.float32)
+    st = np.zeros((8, d["nxx"], d["nzz"]), dtype=np.float32) if want_state else None
+    _check(lib().qpstd_model_shot(C.byref(D.s), _f(g), _f(st)))
+    return (g, st) if want_state else g
+
+
+def rtm_shot(d: dict, obs: np.ndarray, method: int = FUSED):
+    D = Desc(d, method)
+    nx, nz = d["nxx"] - 2 * d["pml"], d["nzz"] - 2 * d["pml"]
+    obs = np.ascontiguousarray(obs, dtype=np.float32)
+    img = np.zeros((nx, nz), dtype=np.float32)
+    ssg = np.zeros((nx, nz), dtype=np.float32)
+    _check(lib().qpstd_rtm_shot(C.byref(D.s), _f(obs), _f(img), _f(ssg)))
+    return img, ssg
+
+
+def filter_image(img: np.ndarray, dx: float, dz: float) -> np.ndarray:
+    img = np.ascontiguousarray(img, dtype=np.float32)
+    out = np.zeros_like(img)
+    _check(lib().qpstd_filter_image(img.shape[0], img.shape[1], dx, dz, _f(img), _f(out)))
+    return out
+
+
+class Shot:
+    """Device-resident shot (qpstd_shot handle)."""
+
+    def __init__(self, d: dict, method: int = FUSED):
+        self.D = Desc(d, method)
+        self.h = C.c_void_p()
+        _check(lib().qpstd_shot_create(C.byref(self.D.s), C.byref(self.h)))
+        self.d = d
+
+    def close(self):
+        if self.h:
+            lib().qpstd_shot_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, st):
+        st = np.ascontiguousarray(st, dtype=np.float32)
+        _check(lib().qpstd_shot_set_state(self.h, _f(st)))
+
+    def get_state(self):
+        st = np.zeros((8, self.d["nxx"], self.d["nzz"]), dtype=np.float32)
+        _check(lib().qpstd_shot_get_state(self.h, _f(st)))
+        return st
+
+    def advance(self, t0: int, n: int, want_gather: bool = True):
+        g = np.zeros((n, self.D.s.nr), dtype=np.float32) if want_gather else None
+        _check(lib().qpstd_shot_advance(self.h, t0, n, _f(g)))
+        return g
+
+    def advance_device(self, t0: int, n: int):
+        _check(lib().qpstd_shot_advance_device(self.h, t0, n))
+
+    def launch_count(self) -> int:
+        return int(lib().qpstd_shot_launch_count(self.h))
+
+    def set_obs(self, obs):
+        obs = np.ascontiguousarray(obs, dtype=np.float32)
+        self._obs = obs
+        _check(lib().qpstd_shot_set_obs(self.h, _f(obs)))
+
+    def rtm_device(self):
+        _check(lib().qpstd_shot_rtm_device(self.h))
+
+    def get_image(self):
+        nx, nz = self.d["nxx"] - 2 * self.d["pml"], self.d["nzz"] - 2 * self.d["pml"]
+        img = np.zeros((nx, nz), dtype=np.float32)
+        ssg = np.zeros((nx, nz), dtype=np.float32)
+        _check(lib().qpstd_shot_get_image(self.h, _f(img), _f(ssg)))
+        return img, ssg
+
+    def forward_steps(self) -> int:
+        return int(lib().qpstd_shot_forward_steps(self.h))
+
+    def sync(self):
+        _check(lib().qpstd_shot_sync(self.h))

@@ -1,0 +1,119 @@
+/*
+ * qpstd.h -- C ABI of the GB300 Constant-Q-PSTD time-stepping library.
+ *
+ * The reference exposes its hot path as one `extern "C" void acforward(...)`
+ * per program, ~40 positional scalars and host pointers, no status code:
+ *   aps  : sgpstd-qmodeling/acps4.cu:184-198   (called acousticsgps4.c:442)
+ *   vaps : sgpstd-qmodeling/acsglw.cu:185-200  (called visacousticsgps4.c:455)
+ *   artm : sgpstd-qrtm/acps4.cu:183-197        (called main.c:458)
+ *   qrtm : sgpstd-qrtm/acsglw.cu:189-204       (called acrtmain.c:459)
+ * Each acforward loops over shots; per shot it windows the model
+ * (select_part_model / expand_pml_areas), places the source and receivers,
+ * time-steps on the GPU and writes the gather (modeling) or accumulates the
+ * image (RTM).  The entry points below are that per-shot body with the
+ * windowing already done by the caller, taking plain host pointers and sizes
+ * and returning a status code; qpstd_acforward_* further down restore the
+ * whole-program signatures.
+ *
+ * Layout conventions (as in the reference): every 2-D array is x-major,
+ * point (ix,iz) at ix*nzz+iz; gathers and observed data are time-major,
+ * sample (t, ir) at t*nr+ir; images are interior nx*nz, x-major.
+ */
+#ifndef QPSTD_H
+#define QPSTD_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define QPSTD_OK 0
+#define QPSTD_EINVAL (-1)    /* bad argument (sizes, indices, null pointers) */
+#define QPSTD_ECUDA (-2)     /* CUDA runtime error (message in qpstd_last_error) */
+#define QPSTD_ENOMEM (-3)    /* device allocation failed */
+#define QPSTD_EREVOLVE (-4)  /* checkpoint schedule error (revolve info code) */
+#define QPSTD_ENOTSUP (-5)   /* combination not built */
+
+/* program kinds (the reference's four executables) */
+#define QPSTD_APS 0   /* acoustic modeling            */
+#define QPSTD_VAPS 1  /* constant-Q modeling          */
+#define QPSTD_ARTM 2  /* acoustic RTM                 */
+#define QPSTD_QRTM 3  /* Q-compensated RTM            */
+
+/* step implementations */
+#define QPSTD_FUSED 0  /* hand-written shared-memory line-FFT passes (default) */
+#define QPSTD_PLAIN 1  /* cuFFT 2-D C2C + elementwise kernels, the reference's step order */
+
+/* One shot on its padded (window + CPML) grid.  All pointers are host memory
+ * owned by the caller and only read during the call. */
+typedef struct qpstd_shot_desc {
+    int kind;                 /* QPSTD_APS .. QPSTD_QRTM */
+    int method;               /* QPSTD_FUSED or QPSTD_PLAIN */
+    int nxx, nzz, pml;        /* padded grid (nx+2*pml, nz+2*pml) and CPML width */
+    float dx, dz;             /* grid spacing (m) */
+    float dt;                 /* time step (s); the reference reads ms and divides by 1000 */
+    float fd;                 /* dominant frequency: CPML alpha_max = pi*fd (funca.c:230) */
+    int nt;                   /* time samples (tmax) */
+    const float *vp, *rho;    /* windowed, PML-expanded models, nxx*nzz */
+    const float *bbx, *bbz;   /* staggered buoyancy, nxx*nzz (cal_bbx_bbz on the full model) */
+    const float *gam, *lam, *vwd, *tao; /* constant-Q fields (transfermodel), VAPS/QRTM only */
+    const float *rik;         /* source wavelet, nt */
+    int xsg, zsg;             /* source grid index on the padded grid */
+    int nr;                   /* receivers */
+    const int *gxg, *gzg;     /* receiver grid indices on the padded grid */
+    float etas, etar;         /* Q-RTM filter stabilisation (x 1e-6 inside, as the reference) */
+    float taoc;               /* Q-RTM filter tau: max tau over the window (acsglw.cu:354-356) */
+    int snaps;                /* RTM checkpoints (revolve snaps), 1..64 */
+} qpstd_shot_desc;
+
+/* Library / device status.  Thread-compatible: one caller per device. */
+const char *qpstd_last_error(void);
+int qpstd_version(void);
+
+/* Modeling of one shot (aps / vaps).  gather: nt*nr floats, p after the
+ * pressure update of each step at the receivers (acps4.cu:568,611-621).
+ * state (optional, NULL to skip): the final p,vx,vz,fipx,fipz,fivxx,fivzz,aux,
+ * 8*nxx*nzz floats.  Replaces the per-shot body of acforward (aps, vaps). */
+int qpstd_model_shot(const qpstd_shot_desc *d, float *gather, float *state);
+
+/* RTM of one shot (artm / qrtm).  obs: nt*nr observed data (direct arrival
+ * already muted, removedirect).  img, ssg: nx*nz (interior) cross-correlation
+ * image and first-sweep source illumination, before the Laplacian filter.
+ * Replaces the per-shot body of acforward (artm, qrtm) up to filter_image. */
+int qpstd_rtm_shot(const qpstd_shot_desc *d, const float *obs, float *img, float *ssg);
+
+/* 5-point Laplacian image filter with the border zeroed, on the device
+ * (filter_image, sgpstd-qrtm/acsglw.cu:1872; the reference's out-of-range
+ * writes are not reproduced).  img, imgf: host nx*nz. */
+int qpstd_filter_image(int nx, int nz, float dx, float dz, const float *img, float *imgf);
+
+/* ---- device-resident shot handle (inputs stay in HBM between calls) ---- */
+typedef struct qpstd_shot qpstd_shot;
+
+/* Uploads the models and builds all coefficient tables and FFT plans. */
+int qpstd_shot_create(const qpstd_shot_desc *d, qpstd_shot **out);
+int qpstd_shot_destroy(qpstd_shot *s);
+/* 8*nxx*nzz host floats in the order of qpstd_model_shot's state. */
+int qpstd_shot_set_state(qpstd_shot *s, const float *state);
+int qpstd_shot_get_state(qpstd_shot *s, float *state);
+/* Advance nsteps steps starting at step index t0 (source wavelet index).
+ * gather (host, may be NULL): nsteps*nr floats. */
+int qpstd_shot_advance(qpstd_shot *s, int t0, int nsteps, float *gather);
+/* Same, leaving the gather in device memory (no host copy, no sync). */
+int qpstd_shot_advance_device(qpstd_shot *s, int t0, int nsteps);
+/* Number of kernels the last advance call launched. */
+long long qpstd_shot_launch_count(const qpstd_shot *s);
+/* Full RTM of the shot with the device-resident observed data uploaded by
+ * qpstd_shot_set_obs; results stay on the device until qpstd_shot_get_image. */
+int qpstd_shot_set_obs(qpstd_shot *s, const float *obs);
+int qpstd_shot_rtm_device(qpstd_shot *s);
+int qpstd_shot_get_image(qpstd_shot *s, float *img, float *ssg);
+/* Forward steps the last RTM executed (revolve recompute included). */
+long long qpstd_shot_forward_steps(const qpstd_shot *s);
+/* Synchronise the shot's stream. */
+int qpstd_shot_sync(qpstd_shot *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QPSTD_H */

@@ -1,0 +1,39 @@
+"""CPU-side checks of the C ABI: the library loads and exports every symbol
+that include/qpstd.h declares (no compute calls without a GPU)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+import qpstd
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for fn in os.listdir(inc):
+        if fn.endswith(".h"):
+            src = open(os.path.join(inc, fn)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names |= set(re.findall(r"\b(qpstd_\w+)\s*\(", src))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol():
+    if not os.path.exists(qpstd.LIB_PATH):
+        qpstd.build()
+    lib = C.CDLL(qpstd.LIB_PATH)
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+    assert len(declared_symbols()) >= 15
+
+
+def test_python_bindings_cover_the_header():
+    assert set(declared_symbols()) <= set(qpstd.EXPORTS)
+
+
+def test_version_without_gpu():
+    assert qpstd.lib().qpstd_version() >= 100
