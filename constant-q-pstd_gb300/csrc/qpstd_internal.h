@@ -74,4 +74,88 @@ struct AcXArgs {
     const float* ps;              // source wavefield p for imaging
 };
 
+// ---------------------------------------------------------------------------
+// Constant-Q (vaps / qrtm) step.  The isotropic fractional symbols
+// (k^2)^(1/32), k^2, (k^2)^(33/32), (k^2)^0.505 and the Q-RTM stabilised
+// filter are not separable, so they run as 2-D transforms split into a z pass
+// (real lines -> half spectra in kz, Hermitian packing of two real lines per
+// complex line) and an x pass over the kz columns of those half spectra.
+// Half spectra are stored x-major: S[ix*nzh + kz], nzh = nzz/2+1.
+// ---------------------------------------------------------------------------
+
+// z pass A: [aux <- z-inverse of the aux spectrum]; Dz, psi_vz, div = Dx+Dz;
+// div -> half spectrum G.
+struct VzArgsA {
+    int nxx, nzz, nzh, L;
+    FFTPlanDev pl;
+    const float2* HzM;
+    const float *i_az, *i_bz;
+    const float2* aux_spec;   // spectrum of the previous step's aux (null: aux already real)
+    float* aux;
+    float *vz, *psi_vz;
+    const float* Dx;
+    float* div;
+    float2* G;
+};
+
+// x pass over half spectra: out_j = F_x^-1[ sym_j(kx,kz) F_x in ] / (nxx nzz).
+//   mode 0: three outputs with (k^2)^(1/32), k^2, (k^2)^(33/32)
+//   mode 1: one output with (k^2)^0.505
+//   mode 2: one output with the Q-RTM stabilised symbol at time t_filter
+struct VxsArgs {
+    int nxx, nzz, nzh, L, mode;
+    FFTPlanDev pl;
+    const float *kx2, *kz2;   // squared wavenumbers (unnormalised)
+    const float2* in;
+    float2 *out0, *out1, *out2;
+    float norm;               // 1/(nxx*nzz)
+    float eta6;               // eta * 1e-6 (mode 2)
+    float tao, dt, tt;        // filter tau, dt, nt*dt (mode 2)
+};
+
+// z pass B: Y2, Y3, Y4 from their spectra; total; total -> half spectrum T.
+struct VzArgsB {
+    int nxx, nzz, nzh, L;
+    FFTPlanDev pl;
+    const float2 *Y2, *Y3, *Y4;
+    const float* div;
+    const float *y1, *y2, *y3c, *y4c;
+    float* total;
+    float2* T;
+};
+
+// z pass C: D from its spectrum; pressure update (+ source, receivers,
+// illumination / imaging / injection); p -> half spectrum P; Pz, psi_pz, vz.
+struct VzArgsC {
+    int nxx, nzz, nzh, L, pml;
+    FFTPlanDev pl;
+    const float2* Dspec;
+    const float* total;
+    const float* aux;
+    float* p;
+    const float *e1, *e2, *e3;
+    float sgn;                // -1 vaps (loss), +1 qrtm (compensation)
+    int xs, zs;
+    float src;
+    const int* rec_off;       // receivers by z-pass tile (gx / (2L))
+    const RecEntry* rec;
+    float* gather_row;
+    const float* obs_row;
+    float *ssg, *ssg_c, *img, *img_c;
+    const float* ps;
+    float2* P;
+    const float2* HzP;
+    const float *h_az, *h_bz, *bbz;
+    float *vz, *psi_pz;
+    float dt;
+};
+
+// z pass that only turns a half spectrum back into a real field.
+struct VzArgsI {
+    int nxx, nzz, nzh, L;
+    FFTPlanDev pl;
+    const float2* spec;
+    float* out;
+};
+
 }  // namespace qp

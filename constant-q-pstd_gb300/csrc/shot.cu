@@ -24,6 +24,12 @@ namespace qp {
 void launch_ac_zpass(const AcZArgs& a, cudaStream_t s);
 void launch_ac_xpass(const AcXArgs& a, cudaStream_t s);
 int ac_set_smem_limits();
+void launch_vz_passA(const VzArgsA& a, cudaStream_t s);
+void launch_vz_xspec(const VxsArgs& a, cudaStream_t s);
+void launch_vz_passB(const VzArgsB& a, cudaStream_t s);
+void launch_vz_passC(const VzArgsC& a, cudaStream_t s);
+void launch_vz_zinv(const VzArgsI& a, cudaStream_t s);
+int vz_set_smem_limits();
 }  // namespace qp
 
 using namespace qp;
@@ -111,42 +117,98 @@ static float* dalloc(qpstd_shot* s, size_t n, int* rc) {
     return p;
 }
 
-static int build_receivers(qpstd_shot* s, const qpstd_shot_desc* d) {
-    const int TZ = 2 * s->Lx;
-    s->ntile_x = (s->d.nzz + TZ - 1) / TZ;
-    std::vector<std::vector<RecEntry>> per(s->ntile_x);
+// Receivers grouped by the CTA tile that owns their cell: x passes tile the z
+// axis (key gz / width), z passes tile the x axis (key gx / width).
+static int build_rec_list(qpstd_shot* s, const qpstd_shot_desc* d, int width, bool key_x, int** off_out,
+                          RecEntry** rec_out) {
+    const int ntile = ((key_x ? d->nxx : d->nzz) + width - 1) / width;
+    std::vector<std::vector<RecEntry>> per(ntile);
     // winning receiver per cell: the reference marks flagrec/rindex per cell,
     // the last receiver written wins (acsglw.cu:387-403)
     std::vector<int> win(d->nr, 1);
     for (int i = 0; i < d->nr; i++)
         for (int j = i + 1; j < d->nr; j++)
-            if (d->gxg[i] == d->gxg[j] && d->gzg[i] == d->gzg[j]) { win[i] = 0; break; }
+            if (d->gxg[i] == d->gxg[j] && d->gzg[i] == d->gzg[j]) {
+                win[i] = 0;
+                break;
+            }
     for (int i = 0; i < d->nr; i++) {
         RecEntry e;
         e.gx = d->gxg[i];
         e.gz = d->gzg[i];
         e.ir = i;
         e.inject = win[i];
-        per[e.gz / TZ].push_back(e);
+        per[(key_x ? e.gx : e.gz) / width].push_back(e);
     }
-    std::vector<int> off(s->ntile_x + 1, 0);
+    std::vector<int> off(ntile + 1, 0);
     std::vector<RecEntry> flat;
-    for (int t = 0; t < s->ntile_x; t++) {
+    for (int t = 0; t < ntile; t++) {
         off[t] = (int)flat.size();
         flat.insert(flat.end(), per[t].begin(), per[t].end());
     }
-    off[s->ntile_x] = (int)flat.size();
+    off[ntile] = (int)flat.size();
     int* doff = nullptr;
     CK(cudaMalloc(&doff, sizeof(int) * off.size()));
     s->allocs.push_back(doff);
     CK(cudaMemcpy(doff, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
-    s->rec_off = doff;
     RecEntry* drec = nullptr;
     const size_t nrec = std::max<size_t>(flat.size(), 1);
     CK(cudaMalloc(&drec, sizeof(RecEntry) * nrec));
     s->allocs.push_back(drec);
     if (!flat.empty()) CK(cudaMemcpy(drec, flat.data(), sizeof(RecEntry) * flat.size(), cudaMemcpyHostToDevice));
-    s->rec = drec;
+    *off_out = doff;
+    *rec_out = drec;
+    return QPSTD_OK;
+}
+
+static int build_receivers(qpstd_shot* s, const qpstd_shot_desc* d) {
+    int rc = build_rec_list(s, d, 2 * s->Lx, false, &s->rec_off, &s->rec);
+    if (rc || !s->visco) return rc;
+    return build_rec_list(s, d, 2 * s->Lzv, true, &s->rec_off_z, &s->rec_z);
+}
+
+// Per-point constant-Q coefficients and the spectra scratch (double -> float once).
+static int setup_visco(qpstd_shot* s, const qpstd_shot_desc* d) {
+    const size_t N = s->N;
+    int rc = QPSTD_OK;
+    const size_t NS = (size_t)d->nxx * s->nzh;  // half-spectrum length (complex)
+    float* f = dalloc(s, 8 * N, &rc);
+    if (!f) return rc;
+    s->y1 = f; s->y2 = f + N; s->y3c = f + 2 * N; s->y4c = f + 3 * N;
+    s->e1 = f + 4 * N; s->e2 = f + 5 * N; s->e3 = f + 6 * N; s->total = f + 7 * N;
+    float* sp = dalloc(s, 2 * NS * (s->rtm ? 6 : 5), &rc);
+    if (!sp) return rc;
+    for (int k = 0; k < 4; k++) s->spec[k] = reinterpret_cast<float2*>(sp) + k * NS;
+    s->src.aux_spec = reinterpret_cast<float2*>(sp) + 4 * NS;
+    if (s->rtm) s->rcv.aux_spec = reinterpret_cast<float2*>(sp) + 5 * NS;
+    std::vector<float> h(7 * N);
+    const double dt = d->dt;
+    for (size_t i = 0; i < N; i++) {
+        const double g = d->gam[i], w = d->vwd[i], vp = d->vp[i], lam = d->lam[i], tao = d->tao[i];
+        const double cc = dt * dt * vp * vp * lam / 12.0;  // sum_total, acsglw.cu:1213-1245
+        h[i] = (float)(1.0 - 32.0 * g);
+        h[N + i] = (float)(32.0 * g * w);
+        h[2 * N + i] = (float)((1.0 - 64.0 * g) * cc);
+        h[3 * N + i] = (float)(64.0 * g * w * cc);
+        h[4 * N + i] = (float)((double)d->rho[i] * vp * vp * dt * lam);  // addsa_kernel, acsglw.cu:1527
+        h[5 * N + i] = (float)(0.5 * dt * tao);
+        h[6 * N + i] = (float)(dt * tao);
+    }
+    CK(cudaMemcpy(f, h.data(), sizeof(float) * 7 * N, cudaMemcpyHostToDevice));
+    std::vector<float> k2(d->nxx + d->nzz);
+    for (int i = 0; i < d->nxx; i++) {
+        const double k = wavenumber(i, d->nxx, d->dx);
+        k2[i] = (float)(k * k);
+    }
+    for (int j = 0; j < d->nzz; j++) {
+        const double k = wavenumber(j, d->nzz, d->dz);
+        k2[d->nxx + j] = (float)(k * k);
+    }
+    float* kk = dalloc(s, k2.size(), &rc);
+    if (!kk) return rc;
+    CK(cudaMemcpy(kk, k2.data(), sizeof(float) * k2.size(), cudaMemcpyHostToDevice));
+    s->kxsq = kk;
+    s->kzsq = kk + d->nxx;
     return QPSTD_OK;
 }
 
@@ -169,10 +231,10 @@ extern "C" int qpstd_shot_create(const qpstd_shot_desc* d, qpstd_shot** out) {
         qpstd_shot_destroy(s);
         return code;
     };
-    if (s->visco && d->method == QPSTD_FUSED) return bail(fail(QPSTD_ENOTSUP, "fused visco step not built yet"));
     if (d->method == QPSTD_PLAIN) return bail(fail(QPSTD_ENOTSUP, "plain method not built yet"));
     static int smem_ok = -1;
-    if (smem_ok != 0) smem_ok = ac_set_smem_limits();
+    if (smem_ok != 0) smem_ok = (ac_set_smem_limits() || vz_set_smem_limits()) ? -1 : 0;
+    s->nzh = nzz / 2 + 1;
     cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
 
@@ -255,9 +317,14 @@ extern "C" int qpstd_shot_create(const qpstd_shot_desc* d, qpstd_shot** out) {
         if ((rc = upload_plan(s, hz, s->pz))) return bail(rc);
         s->Lx = choose_pairs(nzz, s->px.m);
         s->Lzp = choose_pairs(nxx, s->pz.m);
-        if (16.0 * s->px.m > 200 * 1024 || 16.0 * s->pz.m > 200 * 1024)
+        // constant-Q passes hold three line buffers (z pass B, 3-output x-spectral pass)
+        s->Lzv = std::max(1, std::min(s->Lzp, (150 * 1024) / (24 * s->pz.m)));
+        s->Lxs = std::max(1, std::min(8, std::min((s->nzh + 151) / 152, (96 * 1024) / (16 * s->px.m))));
+        s->Lxs3 = std::max(1, std::min(s->Lxs, (150 * 1024) / (24 * s->px.m)));
+        if (24.0 * s->px.m > 200 * 1024 || 24.0 * s->pz.m > 200 * 1024)
             return bail(fail(QPSTD_ENOTSUP, "line too long for one CTA"));
     }
+    if (s->visco && (rc = setup_visco(s, d))) return bail(rc);
     if ((rc = build_receivers(s, d))) return bail(rc);
     s->gather = dalloc(s, (size_t)d->nt * std::max(d->nr, 1), &rc);
     if (!s->gather) return bail(rc);
@@ -278,6 +345,11 @@ extern "C" int qpstd_shot_create(const qpstd_shot_desc* d, qpstd_shot** out) {
 extern "C" int qpstd_shot_destroy(qpstd_shot* s) {
     if (!s) return QPSTD_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
+    for (auto& t : s->timed) {
+        cudaEventDestroy(t.a);
+        cudaEventDestroy(t.b);
+    }
+    for (cudaEvent_t e : s->evpool) cudaEventDestroy(e);
     for (void* p : s->allocs) cudaFree(p);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
@@ -288,6 +360,7 @@ extern "C" int qpstd_shot_set_state(qpstd_shot* s, const float* state) {
     if (!s || !state) return fail(QPSTD_EINVAL, "null argument");
     CK(cudaMemcpyAsync(s->src.st, state, sizeof(float) * 8 * s->N, cudaMemcpyHostToDevice, s->stream));
     CK(cudaStreamSynchronize(s->stream));
+    s->src.aux_pending = false;
     return QPSTD_OK;
 }
 
@@ -297,6 +370,38 @@ extern "C" int qpstd_shot_get_state(qpstd_shot* s, float* state) {
     CK(cudaStreamSynchronize(s->stream));
     return QPSTD_OK;
 }
+
+// ---------------------------------------------------------------------------
+// per-launch timing
+static cudaEvent_t pool_event(qpstd_shot* s) {
+    if (!s->evpool.empty()) {
+        cudaEvent_t e = s->evpool.back();
+        s->evpool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+struct ProfScope {
+    qpstd_shot* s;
+    int kind;
+    cudaEvent_t a = nullptr;
+    ProfScope(qpstd_shot* s_, int k) : s(s_), kind(k) {
+        if (s->prof) {
+            a = pool_event(s);
+            cudaEventRecord(a, s->stream);
+        }
+        s->launches++;
+    }
+    ~ProfScope() {
+        if (s->prof) {
+            cudaEvent_t b = pool_event(s);
+            cudaEventRecord(b, s->stream);
+            s->timed.push_back({kind, a, b});
+        }
+    }
+};
 
 // ---------------------------------------------------------------------------
 // acoustic passes
@@ -361,33 +466,185 @@ static AcXArgs xargs(qpstd_shot* s, Wave& w, int do_p, int do_v, int do_dx) {
     return a;
 }
 
+// The source wavefield runs as a pipeline: begin() computes the x part of the
+// first step's divergence, each step() is one z pass and one x pass (the x
+// pass also prepares the next step's x divergence unless it is the last), and
+// end() applies the last step's pending z-velocity update.  Between end() and
+// the next begin() the eight state fields are exactly the reference's state.
+static void src_begin(qpstd_shot* s) {
+    ProfScope ps(s, QPSTD_K_XPASS);
+    launch_ac_xpass(xargs(s, s->src, 0, 0, 1), s->stream);
+}
+
+// One constant-Q step of wavefield w (seven launches, see vz_kernels.cu).
+// src: amplitude at the source this step; t_filter / eta: time index and
+// stabilisation of the Q-RTM aux filter; last: skip the next step's Dx;
+// gather_row / obs_row / ssg_on / image: receiver recording, Dirichlet
+// injection, illumination and imaging, all inside z pass C.
+static void vz_step(qpstd_shot* s, Wave& w, float src, int t_filter, float eta, bool last, float* gather_row,
+                    const float* obs_row, bool ssg_on, bool image) {
+    const size_t N = s->N;
+    cudaStream_t st = s->stream;
+    const int nxx = s->d.nxx, nzz = s->d.nzz, nzh = s->nzh;
+    const float norm = (float)(1.0 / ((double)nxx * nzz));
+    {
+        VzArgsA a{};
+        a.nxx = nxx; a.nzz = nzz; a.nzh = nzh; a.L = s->Lzv; a.pl = s->pz;
+        a.HzM = s->HzM; a.i_az = s->i_az; a.i_bz = s->i_bz;
+        a.aux_spec = w.aux_pending ? w.aux_spec : nullptr;
+        a.aux = w.aux(N); a.vz = w.vz(N); a.psi_vz = w.fivzz(N); a.Dx = w.Dx(N);
+        a.div = s->div; a.G = s->spec[0];
+        ProfScope ps(s, QPSTD_K_ZPASS);
+        launch_vz_passA(a, st);
+        w.aux_pending = false;
+    }
+    VxsArgs xs{};
+    xs.nxx = nxx; xs.nzz = nzz; xs.nzh = nzh; xs.pl = s->px; xs.kx2 = s->kxsq; xs.kz2 = s->kzsq; xs.norm = norm;
+    {
+        VxsArgs a = xs;
+        a.mode = 0; a.L = s->Lxs3;
+        a.in = s->spec[0]; a.out0 = s->spec[1]; a.out1 = s->spec[2]; a.out2 = s->spec[3];
+        ProfScope ps(s, QPSTD_K_XSPEC);
+        launch_vz_xspec(a, st);
+    }
+    {
+        VzArgsB a{};
+        a.nxx = nxx; a.nzz = nzz; a.nzh = nzh; a.L = s->Lzv; a.pl = s->pz;
+        a.Y2 = s->spec[1]; a.Y3 = s->spec[2]; a.Y4 = s->spec[3];
+        a.div = s->div; a.y1 = s->y1; a.y2 = s->y2; a.y3c = s->y3c; a.y4c = s->y4c;
+        a.total = s->total; a.T = s->spec[0];
+        ProfScope ps(s, QPSTD_K_ZPASS);
+        launch_vz_passB(a, st);
+    }
+    {
+        VxsArgs a = xs;
+        a.mode = 1; a.L = s->Lxs;
+        a.in = s->spec[0]; a.out0 = s->spec[1];
+        ProfScope ps(s, QPSTD_K_XSPEC);
+        launch_vz_xspec(a, st);
+    }
+    {
+        VzArgsC a{};
+        a.nxx = nxx; a.nzz = nzz; a.nzh = nzh; a.L = s->Lzv; a.pml = s->d.pml; a.pl = s->pz;
+        a.Dspec = s->spec[1]; a.total = s->total; a.aux = w.aux(N); a.p = w.p(N);
+        a.e1 = s->e1; a.e2 = s->e2; a.e3 = s->e3;
+        a.sgn = (s->d.kind == QPSTD_QRTM) ? 1.f : -1.f;
+        a.xs = (src != 0.f) ? s->d.xsg : -1; a.zs = s->d.zsg; a.src = src;
+        if (gather_row || obs_row) { a.rec_off = s->rec_off_z; a.rec = s->rec_z; }
+        a.gather_row = gather_row; a.obs_row = obs_row;
+        if (ssg_on) { a.ssg = s->ssg; a.ssg_c = s->ssg_c; }
+        if (image) { a.img = s->img; a.img_c = s->img_c; a.ps = s->src.p(N); }
+        a.P = s->spec[2]; a.HzP = s->HzP; a.h_az = s->h_az; a.h_bz = s->h_bz; a.bbz = s->bbz;
+        a.vz = w.vz(N); a.psi_pz = w.fipz(N); a.dt = s->d.dt;
+        ProfScope ps(s, QPSTD_K_ZPASS);
+        launch_vz_passC(a, st);
+    }
+    {
+        ProfScope ps(s, QPSTD_K_XPASS);
+        launch_ac_xpass(xargs(s, w, 0, 1, last ? 0 : 1), st);
+    }
+    {
+        VxsArgs a = xs;
+        a.L = s->Lxs;
+        a.in = s->spec[2]; a.out0 = w.aux_spec;
+        if (s->d.kind == QPSTD_QRTM) {
+            // multt_kernel, sgpstd-qrtm/acsglw.cu:1895: eta scaled by 1e-6, tt = nt*dt in float
+            a.mode = 2; a.eta6 = (float)((double)eta * 1e-6); a.tao = s->d.taoc; a.dt = s->d.dt;
+            a.tt = (float)t_filter * s->d.dt;
+        } else {
+            a.mode = 1;
+        }
+        ProfScope ps(s, QPSTD_K_XSPEC);
+        launch_vz_xspec(a, st);
+        w.aux_pending = true;
+    }
+}
+
+// Turn a pending aux spectrum back into the real aux field.
+static void vz_finish(qpstd_shot* s, Wave& w) {
+    if (!w.aux_pending) return;
+    VzArgsI a{};
+    a.nxx = s->d.nxx; a.nzz = s->d.nzz; a.nzh = s->nzh; a.L = s->Lzv; a.pl = s->pz;
+    a.spec = w.aux_spec; a.out = w.aux(s->N);
+    ProfScope ps(s, QPSTD_K_ZPASS);
+    launch_vz_zinv(a, s->stream);
+    w.aux_pending = false;
+}
+
+static float src_amp(qpstd_shot* s, int t) {
+    return (t >= 0 && t < s->d.nt) ? (float)((double)s->rik[t] * s->d.dt * 1000.0) : 0.f;
+}
+
+// One step at source-wavelet index t.  first: no pending vz update;
+// gather_row: device row for the receivers (or null); ssg_on: accumulate the
+// illumination (first sweep of RTM, addsa_kernel restart==0).
+static void src_step(qpstd_shot* s, int t, bool first, bool last, float* gather_row, bool ssg_on) {
+    Wave& w = s->src;
+    if (s->visco) {
+        vz_step(s, w, src_amp(s, t), t, s->d.etas, last, gather_row, nullptr, ssg_on, false);
+        return;
+    }
+    {
+        ProfScope ps(s, QPSTD_K_ZPASS);
+        launch_ac_zpass(zargs(s, w, first ? 0 : 1, 1), s->stream);
+    }
+    AcXArgs x = xargs(s, w, 1, 1, last ? 0 : 1);
+    x.xs = s->d.xsg;
+    x.zs = s->d.zsg;
+    x.src = src_amp(s, t);
+    x.rec_off = s->rec_off;
+    x.rec = s->rec;
+    x.gather_row = gather_row;
+    if (ssg_on) {
+        x.ssg = s->ssg;
+        x.ssg_c = s->ssg_c;
+    }
+    ProfScope ps(s, QPSTD_K_XPASS);
+    launch_ac_xpass(x, s->stream);
+}
+
+static void src_end(qpstd_shot* s) {
+    if (s->visco) {
+        vz_finish(s, s->src);
+        return;
+    }
+    ProfScope ps(s, QPSTD_K_ZPASS);
+    launch_ac_zpass(zargs(s, s->src, 1, 0), s->stream);
+}
+
 // Advance the source wavefield over steps t0 .. t0+n-1 (source wavelet index t).
-// gather: device rows for each step (row t-t0), or null.  ssg_on: accumulate
-// the illumination (first sweep of RTM, addsa_kernel restart==0).
+// gather: device rows for each step (row t-t0), or null.
 static int advance_src(qpstd_shot* s, int t0, int n, float* gather, bool ssg_on) {
     if (n <= 0) return QPSTD_OK;
-    Wave& w = s->src;
-    cudaStream_t st = s->stream;
-    launch_ac_xpass(xargs(s, w, 0, 0, 1), st);
-    s->launches++;
-    for (int t = t0; t < t0 + n; t++) {
-        launch_ac_zpass(zargs(s, w, t > t0, 1), st);
-        AcXArgs x = xargs(s, w, 1, 1, t < t0 + n - 1);
-        x.xs = s->d.xsg;
-        x.zs = s->d.zsg;
-        x.src = (t < s->d.nt) ? (float)((double)s->rik[t] * s->d.dt * 1000.0) : 0.f;
-        x.rec_off = s->rec_off;
-        x.rec = s->rec;
-        x.gather_row = gather ? gather + (size_t)(t - t0) * s->d.nr : nullptr;
-        if (ssg_on) {
-            x.ssg = s->ssg;
-            x.ssg_c = s->ssg_c;
-        }
-        launch_ac_xpass(x, st);
-        s->launches += 2;
-    }
-    launch_ac_zpass(zargs(s, w, 1, 0), st);
-    s->launches++;
+    src_begin(s);
+    for (int t = t0; t < t0 + n; t++)
+        src_step(s, t, t == t0, t == t0 + n - 1, gather ? gather + (size_t)(t - t0) * s->d.nr : nullptr, ssg_on);
+    src_end(s);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    return QPSTD_OK;
+}
+
+extern "C" int qpstd_shot_pipeline_begin(qpstd_shot* s) {
+    if (!s) return fail(QPSTD_EINVAL, "null shot");
+    s->launches = 0;
+    s->pipe_first = true;
+    src_begin(s);
+    return QPSTD_OK;
+}
+
+extern "C" int qpstd_shot_pipeline_step(qpstd_shot* s, int t, int last) {
+    if (!s || t < 0) return fail(QPSTD_EINVAL, "bad pipeline step");
+    src_step(s, t, s->pipe_first, last != 0, nullptr, false);
+    s->pipe_first = false;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    return QPSTD_OK;
+}
+
+extern "C" int qpstd_shot_pipeline_end(qpstd_shot* s) {
+    if (!s) return fail(QPSTD_EINVAL, "null shot");
+    src_end(s);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
     return QPSTD_OK;
@@ -400,7 +657,17 @@ static int advance_src(qpstd_shot* s, int t0, int n, float* gather, bool ssg_on)
 static int receiver_step(qpstd_shot* s, int row, bool first) {
     Wave& w = s->rcv;
     cudaStream_t st = s->stream;
-    launch_ac_zpass(zargs(s, w, first ? 0 : 1, 1), st);
+    if (s->visco) {
+        // addsa_b_kernel + multt_kernel(etar, nt = row), sgpstd-qrtm/acsglw.cu:745-776, 907-940
+        vz_step(s, w, 0.f, row, s->d.etar, false, nullptr, s->obs + (size_t)row * s->d.nr, false, true);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+        return QPSTD_OK;
+    }
+    {
+        ProfScope ps(s, QPSTD_K_ZPASS);
+        launch_ac_zpass(zargs(s, w, first ? 0 : 1, 1), st);
+    }
     AcXArgs x = xargs(s, w, 1, 1, 1);
     x.rec_off = s->rec_off;
     x.rec = s->rec;
@@ -408,8 +675,10 @@ static int receiver_step(qpstd_shot* s, int row, bool first) {
     x.img = s->img;
     x.img_c = s->img_c;
     x.ps = s->src.p(s->N);
-    launch_ac_xpass(x, st);
-    s->launches += 2;
+    {
+        ProfScope ps(s, QPSTD_K_XPASS);
+        launch_ac_xpass(x, st);
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
     return QPSTD_OK;
@@ -432,6 +701,35 @@ extern "C" int qpstd_shot_advance(qpstd_shot* s, int t0, int nsteps, float* gath
 }
 
 extern "C" long long qpstd_shot_launch_count(const qpstd_shot* s) { return s ? s->launches : -1; }
+
+extern "C" void* qpstd_shot_stream(qpstd_shot* s) { return s ? (void*)s->stream : nullptr; }
+
+extern "C" int qpstd_shot_set_profiling(qpstd_shot* s, int on) {
+    if (!s) return fail(QPSTD_EINVAL, "null shot");
+    s->prof = on != 0;
+    return QPSTD_OK;
+}
+
+extern "C" int qpstd_shot_profile_read(qpstd_shot* s, int nkinds, double* ms, long long* count) {
+    if (!s || nkinds < 1 || !ms || !count) return fail(QPSTD_EINVAL, "bad profile arguments");
+    CK(cudaStreamSynchronize(s->stream));
+    for (int k = 0; k < nkinds; k++) {
+        ms[k] = 0.0;
+        count[k] = 0;
+    }
+    for (auto& t : s->timed) {
+        float v = 0.f;
+        cudaEventElapsedTime(&v, t.a, t.b);
+        if (t.kind >= 0 && t.kind < nkinds) {
+            ms[t.kind] += v;
+            count[t.kind] += 1;
+        }
+        s->evpool.push_back(t.a);
+        s->evpool.push_back(t.b);
+    }
+    s->timed.clear();
+    return QPSTD_OK;
+}
 extern "C" long long qpstd_shot_forward_steps(const qpstd_shot* s) { return s ? s->fwd_steps : -1; }
 extern "C" int qpstd_shot_sync(qpstd_shot* s) {
     if (!s) return fail(QPSTD_EINVAL, "null shot");
@@ -458,6 +756,7 @@ extern "C" int qpstd_shot_rtm_device(qpstd_shot* s) {
     CK(cudaMemsetAsync(s->src.st, 0, sizeof(float) * 9 * N, st));
     CK(cudaMemsetAsync(s->rcv.st, 0, sizeof(float) * 9 * N, st));
     CK(cudaMemsetAsync(s->img, 0, sizeof(float) * 4 * NI, st));
+    s->src.aux_pending = s->rcv.aux_pending = false;
     Revolve rv(s->d.nt, s->d.snaps);
     int ts = 0, rc;
     bool first_sweep = true, first_rcv = true;
@@ -468,9 +767,9 @@ extern "C" int qpstd_shot_rtm_device(qpstd_shot* s) {
             CK(cudaMemcpyAsync(slot, s->src.st, sizeof(float) * 8 * N, cudaMemcpyDeviceToDevice, st));
             if (rv.capo() == 0) {
                 // checkpoint 0 also holds the first source sample (acsglw.cu:493-500)
+                ProfScope ps(s, QPSTD_K_OTHER);
                 add_point_kernel<<<1, 1, 0, st>>>(slot + (size_t)s->d.xsg * s->d.nzz + s->d.zsg,
                                                   (float)((double)s->rik[0] * 1000.0 * s->d.dt));
-                s->launches++;
             }
         } else if (act == RV_ADVANCE) {
             const int n = rv.capo() - ts + 1;
@@ -485,6 +784,7 @@ extern "C" int qpstd_shot_rtm_device(qpstd_shot* s) {
         } else if (act == RV_RESTORE) {
             const float* slot = s->store + (size_t)rv.check() * 8 * N;
             CK(cudaMemcpyAsync(s->src.st, slot, sizeof(float) * 8 * N, cudaMemcpyDeviceToDevice, st));
+            s->src.aux_pending = false;
             ts = rv.capo() + 1;
         } else if (act == RV_TERMINATE) {
             break;

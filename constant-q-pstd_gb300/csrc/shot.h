@@ -24,6 +24,10 @@ struct Wave {
     float* fivzz(size_t N) { return st + 6 * N; }
     float* aux(size_t N) { return st + 7 * N; }
     float* Dx(size_t N) { return st + 8 * N; }
+    // constant-Q: spectrum of the aux field produced at the end of a step;
+    // aux_pending means the real aux field has not been refreshed from it yet
+    float2* aux_spec = nullptr;
+    bool aux_pending = false;
 };
 
 }  // namespace qp
@@ -46,10 +50,25 @@ struct qpstd_shot {
     int Lx = 1, Lzp = 1, ntile_x = 0;
     int* rec_off = nullptr;
     qp::RecEntry* rec = nullptr;
+    // constant-Q step
+    int nzh = 0, Lzv = 1, Lxs = 1, Lxs3 = 1;
+    float2* spec[4] = {nullptr, nullptr, nullptr, nullptr};
+    float* total = nullptr;
+    float *y1 = nullptr, *y2 = nullptr, *y3c = nullptr, *y4c = nullptr;
+    float *e1 = nullptr, *e2 = nullptr, *e3 = nullptr;
+    float *kxsq = nullptr, *kzsq = nullptr;   // unnormalised squared wavenumbers
+    int* rec_off_z = nullptr;                  // receivers keyed by z-pass tile
+    qp::RecEntry* rec_z = nullptr;
     std::vector<float> rik;
     float* gather = nullptr;
     float* store = nullptr;
     float* obs = nullptr;
     float *img = nullptr, *img_c = nullptr, *ssg = nullptr, *ssg_c = nullptr;
     long long launches = 0, fwd_steps = 0;
+    // optional per-launch timing (CUDA events on the shot stream)
+    bool pipe_first = true;
+    bool prof = false;
+    struct Timed { int kind; cudaEvent_t a, b; };
+    std::vector<Timed> timed;
+    std::vector<cudaEvent_t> evpool;
 };

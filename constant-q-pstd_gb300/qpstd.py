@@ -68,7 +68,14 @@ EXPORTS = {
     "qpstd_shot_get_image": (C.c_int, [C.c_void_p, _fp, _fp]),
     "qpstd_shot_forward_steps": (C.c_longlong, [C.c_void_p]),
     "qpstd_shot_sync": (C.c_int, [C.c_void_p]),
+    "qpstd_shot_stream": (C.c_void_p, [C.c_void_p]),
+    "qpstd_shot_pipeline_begin": (C.c_int, [C.c_void_p]),
+    "qpstd_shot_pipeline_step": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "qpstd_shot_pipeline_end": (C.c_int, [C.c_void_p]),
+    "qpstd_shot_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "qpstd_shot_profile_read": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
 }
+KIND_NAMES = ["xpass", "zpass", "xspec", "other"]
 
 
 def lib():
@@ -207,3 +214,25 @@ class Shot:
 
     def sync(self):
         _check(lib().qpstd_shot_sync(self.h))
+
+    def pipeline_begin(self):
+        _check(lib().qpstd_shot_pipeline_begin(self.h))
+
+    def pipeline_step(self, t: int, last: bool = False):
+        _check(lib().qpstd_shot_pipeline_step(self.h, t, 1 if last else 0))
+
+    def pipeline_end(self):
+        _check(lib().qpstd_shot_pipeline_end(self.h))
+
+    def stream_ptr(self) -> int:
+        return int(lib().qpstd_shot_stream(self.h) or 0)
+
+    def set_profiling(self, on: bool):
+        _check(lib().qpstd_shot_set_profiling(self.h, 1 if on else 0))
+
+    def profile_read(self):
+        n = len(KIND_NAMES)
+        ms = (C.c_double * n)()
+        cnt = (C.c_longlong * n)()
+        _check(lib().qpstd_shot_profile_read(self.h, n, ms, cnt))
+        return {KIND_NAMES[k]: (ms[k], cnt[k]) for k in range(n)}

@@ -101,7 +101,14 @@ int qpstd_shot_get_state(qpstd_shot *s, float *state);
 int qpstd_shot_advance(qpstd_shot *s, int t0, int nsteps, float *gather);
 /* Same, leaving the gather in device memory (no host copy, no sync). */
 int qpstd_shot_advance_device(qpstd_shot *s, int t0, int nsteps);
-/* Number of kernels the last advance call launched. */
+/* The same steps as a caller-driven pipeline (for streaming and timing):
+ * begin() prepares the first step, each step(t, last) runs one time step at
+ * source-wavelet index t (last=1 on the final one), end() completes the last
+ * step.  Only after end() does the state equal the reference's. */
+int qpstd_shot_pipeline_begin(qpstd_shot *s);
+int qpstd_shot_pipeline_step(qpstd_shot *s, int t, int last);
+int qpstd_shot_pipeline_end(qpstd_shot *s);
+/* Number of kernels launched since the last advance / RTM / pipeline_begin. */
 long long qpstd_shot_launch_count(const qpstd_shot *s);
 /* Full RTM of the shot with the device-resident observed data uploaded by
  * qpstd_shot_set_obs; results stay on the device until qpstd_shot_get_image. */
@@ -112,6 +119,19 @@ int qpstd_shot_get_image(qpstd_shot *s, float *img, float *ssg);
 long long qpstd_shot_forward_steps(const qpstd_shot *s);
 /* Synchronise the shot's stream. */
 int qpstd_shot_sync(qpstd_shot *s);
+/* The shot's CUDA stream (cudaStream_t), for callers that order or time work on it. */
+void *qpstd_shot_stream(qpstd_shot *s);
+
+/* Per-launch timing: while on, every kernel launch of the shot is bracketed by
+ * CUDA events on its stream; profile_read synchronises and returns, per kernel
+ * kind, the summed milliseconds and the launch count, then clears the record. */
+#define QPSTD_K_XPASS 0   /* x-line pass (real fields) */
+#define QPSTD_K_ZPASS 1   /* z-line pass (real fields) */
+#define QPSTD_K_XSPEC 2   /* x-line pass over z-spectra (2-D isotropic operators) */
+#define QPSTD_K_OTHER 3   /* small helpers (checkpoint-0 source sample, filters) */
+#define QPSTD_NKINDS 4
+int qpstd_shot_set_profiling(qpstd_shot *s, int on);
+int qpstd_shot_profile_read(qpstd_shot *s, int nkinds, double *ms, long long *count);
 
 #ifdef __cplusplus
 }
