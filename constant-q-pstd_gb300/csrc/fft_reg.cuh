@@ -1,0 +1,313 @@
+// fft_reg.cuh -- register-blocked line FFT for the PSTD pass kernels.
+//
+// A CTA of TX x L threads holds L complex lines (stride ld float2) in shared
+// memory; thread (x, y) works on line y.  A length-m transform is a sequence
+// of Stockham passes of radix R <= 16; in a pass every active thread loads the
+// R inputs of one butterfly into registers, applies the twiddles, runs an
+// in-register DFT of size R (nested Cooley-Tukey with compile-time roots of
+// unity), and after a barrier stores the R outputs in place.  TX is chosen so
+// that one butterfly per thread covers the line (TX >= m / min R).
+//
+// Lengths with a prime factor above 13 use Bluestein's identity with a
+// {2,3,5,7}-smooth inner length m >= 2n-1 (the k-grid stays the reference's,
+// cufftPlan2d on the window, sgpstd-qmodeling/acps4.cu:871).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "qpstd_internal.h"
+
+namespace qp {
+
+// ---- complex helpers ----------------------------------------------------------
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+
+// ---- compile-time roots of unity (Taylor series, evaluated by the compiler) ----
+constexpr double kPiD = 3.14159265358979323846264338327950288;
+constexpr double ct_cos(double x) {
+    double term = 1.0, sum = 1.0;
+    for (int i = 1; i < 40; i++) {
+        term *= -x * x / ((2.0 * i - 1.0) * (2.0 * i));
+        sum += term;
+    }
+    return sum;
+}
+constexpr double ct_sin(double x) {
+    double term = x, sum = x;
+    for (int i = 1; i < 40; i++) {
+        term *= -x * x / ((2.0 * i) * (2.0 * i + 1.0));
+        sum += term;
+    }
+    return sum;
+}
+// c[m] + i s[m] = exp(2 pi i m / R)
+template <int R> struct Roots {
+    float c[R];
+    float s[R];
+    constexpr Roots() : c(), s() {
+        for (int m = 0; m < R; m++) {
+            double a = 2.0 * kPiD * m / R;
+            if (a > kPiD) a -= 2.0 * kPiD;
+            c[m] = (float)ct_cos(a);
+            s[m] = (float)ct_sin(a);
+        }
+    }
+};
+
+template <int R> constexpr int small_factor() {
+    for (int f = 2; f * f <= R; f++)
+        if (R % f == 0) return f;
+    return R;
+}
+
+// ---- in-register DFTs, S = -1 forward (e^{-i}), +1 inverse ---------------------
+template <int R, int S> __device__ __forceinline__ void dft(float2 (&v)[R]);
+
+template <int P, int S> __device__ __forceinline__ void dft_prime(float2 (&v)[P]) {
+    if constexpr (P == 2) {
+        const float2 a = v[0], b = v[1];
+        v[0] = cadd(a, b);
+        v[1] = csub(a, b);
+    } else {
+        constexpr int H = (P - 1) / 2;
+        constexpr Roots<P> rt{};
+        float2 a[H], b[H];
+#pragma unroll
+        for (int r = 1; r <= H; r++) {
+            a[r - 1] = cadd(v[r], v[P - r]);
+            b[r - 1] = csub(v[r], v[P - r]);
+        }
+        const float2 x0 = v[0];
+        float2 s0 = x0;
+#pragma unroll
+        for (int r = 0; r < H; r++) s0 = cadd(s0, a[r]);
+#pragma unroll
+        for (int q = 1; q <= H; q++) {
+            float2 re = x0, im = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int r = 1; r <= H; r++) {
+                const int m = (r * q) % P;
+                re.x = fmaf(a[r - 1].x, rt.c[m], re.x);
+                re.y = fmaf(a[r - 1].y, rt.c[m], re.y);
+                im.x = fmaf(b[r - 1].x, rt.s[m], im.x);
+                im.y = fmaf(b[r - 1].y, rt.s[m], im.y);
+            }
+            // + S i im
+            const float2 ii = make_float2(-(float)S * im.y, (float)S * im.x);
+            v[q] = cadd(re, ii);
+            v[P - q] = csub(re, ii);
+        }
+        v[0] = s0;
+    }
+}
+
+template <int R, int S> __device__ __forceinline__ void dft(float2 (&v)[R]) {
+    if constexpr (R == 1) {
+        return;
+    } else if constexpr (R == 4) {
+        const float2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+        const float2 d = csub(v[1], v[3]);
+        const float2 t2 = cadd(v[1], v[3]);
+        const float2 t3 = make_float2(-(float)S * d.y, (float)S * d.x);
+        v[0] = cadd(t0, t2);
+        v[2] = csub(t0, t2);
+        v[1] = cadd(t1, t3);
+        v[3] = csub(t1, t3);
+    } else if constexpr (small_factor<R>() == R) {
+        dft_prime<R, S>(v);
+    } else {
+        // R = A * B, A the smallest factor (R = 8, 16 split as 4 * ...)
+        constexpr int A0 = small_factor<R>();
+        constexpr int A = (A0 == 2 && R % 4 == 0 && R > 4) ? 4 : A0;
+        constexpr int B = R / A;
+        constexpr Roots<R> rt{};
+        float2 u[A][B];
+#pragma unroll
+        for (int a = 0; a < A; a++) {
+#pragma unroll
+            for (int b = 0; b < B; b++) u[a][b] = v[a + A * b];
+            dft<B, S>(u[a]);
+        }
+#pragma unroll
+        for (int a = 1; a < A; a++)
+#pragma unroll
+            for (int q = 1; q < B; q++) {
+                const int m = (a * q) % R;
+                u[a][q] = cmul(u[a][q], make_float2(rt.c[m], (float)S * rt.s[m]));
+            }
+#pragma unroll
+        for (int q = 0; q < B; q++) {
+            float2 t[A];
+#pragma unroll
+            for (int a = 0; a < A; a++) t[a] = u[a][q];
+            dft<A, S>(t);
+#pragma unroll
+            for (int p = 0; p < A; p++) v[q + B * p] = t[p];
+        }
+    }
+}
+
+// ---- one Stockham pass over the lines of the CTA (in place) ------------------------
+// Thread (threadIdx.x, threadIdx.y) handles butterfly j = threadIdx.x of line
+// threadIdx.y.  Ends with a barrier.
+template <int R, int S>
+__device__ __noinline__ void reg_pass(float2* buf, int ld, const FFTPass ps, const float2* __restrict__ tw,
+                                         int L) {
+    const int j = threadIdx.x;
+    const int l = threadIdx.y;
+    const bool act = (j < ps.B) && (l < L);
+    float2 v[R];
+    int k = 0;
+    float2* line = buf + l * ld;
+    if (act) {
+        k = (ps.ns == 1) ? 0 : (int)(j - __umulhi((unsigned)j, ps.ns_magic) * ps.ns);
+#pragma unroll
+        for (int r = 0; r < R; r++) v[r] = line[j + r * ps.B];
+        if (ps.ns > 1) {
+            float2 w1 = __ldg(&tw[k * ps.twstride]);
+            if (S > 0) w1.y = -w1.y;
+            float2 w = w1;
+#pragma unroll
+            for (int r = 1; r < R; r++) {
+                v[r] = cmul(v[r], w);
+                if (r + 1 < R) w = cmul(w, w1);
+            }
+        }
+        dft<R, S>(v);
+    }
+    __syncthreads();
+    if (act) {
+        const int base = (j - k) * R + k;
+#pragma unroll
+        for (int r = 0; r < R; r++) line[base + r * ps.ns] = v[r];
+    }
+    __syncthreads();
+}
+
+// Length-m transform (unnormalised) of the L lines, in place.  One call per
+// transform: the pass loop and its radix switch live in this function, so the
+// kernels that use it hold a single copy of every radix.
+template <int S>
+__device__ __forceinline__ void fft_m_impl(float2* buf, int ld, const FFTPass* __restrict__ sp, int nst,
+                                        const float2* __restrict__ tw, int L) {
+    for (int i = 0; i < nst; i++) {
+        const FFTPass ps = sp[i];
+        switch (ps.R) {
+            case 2: reg_pass<2, S>(buf, ld, ps, tw, L); break;
+            case 3: reg_pass<3, S>(buf, ld, ps, tw, L); break;
+            case 4: reg_pass<4, S>(buf, ld, ps, tw, L); break;
+            case 5: reg_pass<5, S>(buf, ld, ps, tw, L); break;
+            case 6: reg_pass<6, S>(buf, ld, ps, tw, L); break;
+            case 7: reg_pass<7, S>(buf, ld, ps, tw, L); break;
+            case 8: reg_pass<8, S>(buf, ld, ps, tw, L); break;
+            case 9: reg_pass<9, S>(buf, ld, ps, tw, L); break;
+            case 10: reg_pass<10, S>(buf, ld, ps, tw, L); break;
+            case 11: reg_pass<11, S>(buf, ld, ps, tw, L); break;
+            case 12: reg_pass<12, S>(buf, ld, ps, tw, L); break;
+            case 13: reg_pass<13, S>(buf, ld, ps, tw, L); break;
+            case 14: reg_pass<14, S>(buf, ld, ps, tw, L); break;
+            case 15: reg_pass<15, S>(buf, ld, ps, tw, L); break;
+            default: reg_pass<16, S>(buf, ld, ps, tw, L); break;
+        }
+    }
+}
+
+// The plan as the kernels use it: scalars in registers, passes in shared memory.
+struct FFTCtx {
+    int n, m, blue, nst;
+    const FFTPass* sp;
+    const float2 *w, *chirp, *bhat;
+};
+
+// Copies the plan's passes to shared memory (constant indices, so the plan
+// stays in the parameter bank); ends with a barrier.
+__device__ __forceinline__ FFTCtx make_ctx(const FFTPlanDev& pl, FFTPass* s_pass) {
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+#pragma unroll
+    for (int i = 0; i < QP_MAXST; i++)
+        if (t == i && i < pl.nst) s_pass[i] = pl.pass[i];
+    __syncthreads();
+    FFTCtx c;
+    c.n = pl.n;
+    c.m = pl.m;
+    c.blue = pl.blue;
+    c.nst = pl.nst;
+    c.sp = s_pass;
+    c.w = pl.w;
+    c.chirp = pl.chirp;
+    c.bhat = pl.bhat;
+    return c;
+}
+
+template <int S> __device__ __forceinline__ void fft_m(float2* buf, int ld, const FFTCtx& pl, int L) {
+    fft_m_impl<S>(buf, ld, pl.sp, pl.nst, pl.w, L);
+}
+
+// Exact length-n DFT of entries [0,n) of each line, in place.  Caller has
+// synchronised after filling buf; ends with a barrier.
+template <int S> __device__ __forceinline__ void dft_n(float2* buf, int ld, const FFTCtx& pl, int L) {
+    if (!pl.blue) {
+        fft_m<S>(buf, ld, pl, L);
+        return;
+    }
+    const int n = pl.n, m = pl.m;
+    const int l = threadIdx.y;
+    float2* line = buf + l * ld;
+    const bool act = l < L;
+    // inverse = conj(DFT(conj(x)))
+    if (act)
+        for (int k = threadIdx.x; k < m; k += blockDim.x) {
+            float2 v = make_float2(0.f, 0.f);
+            if (k < n) {
+                float2 x = line[k];
+                if (S > 0) x.y = -x.y;
+                v = cmul(x, __ldg(&pl.chirp[k]));
+            }
+            line[k] = v;
+        }
+    __syncthreads();
+    fft_m<-1>(buf, ld, pl, L);
+    if (act)
+        for (int k = threadIdx.x; k < m; k += blockDim.x) line[k] = cmul(line[k], __ldg(&pl.bhat[k]));
+    __syncthreads();
+    fft_m<+1>(buf, ld, pl, L);
+    if (act)
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            float2 y = cmul(line[k], __ldg(&pl.chirp[k]));
+            if (S > 0) y.y = -y.y;
+            line[k] = y;
+        }
+    __syncthreads();
+}
+
+// y = IDFT(H .* DFT(x)) with a complex symbol (length n, 1/n folded in).
+__device__ __forceinline__ void roundtrip_c(float2* buf, int ld, const FFTCtx& pl, int L,
+                                            const float2* __restrict__ H) {
+    dft_n<-1>(buf, ld, pl, L);
+    if (threadIdx.y < L) {
+        float2* line = buf + threadIdx.y * ld;
+        for (int k = threadIdx.x; k < pl.n; k += blockDim.x) line[k] = cmul(line[k], __ldg(&H[k]));
+    }
+    __syncthreads();
+    dft_n<+1>(buf, ld, pl, L);
+}
+
+// Same with a real symbol.
+__device__ __forceinline__ void roundtrip_r(float2* buf, int ld, const FFTCtx& pl, int L,
+                                            const float* __restrict__ H) {
+    dft_n<-1>(buf, ld, pl, L);
+    if (threadIdx.y < L) {
+        float2* line = buf + threadIdx.y * ld;
+        for (int k = threadIdx.x; k < pl.n; k += blockDim.x) line[k] = cscale(line[k], __ldg(&H[k]));
+    }
+    __syncthreads();
+    dft_n<+1>(buf, ld, pl, L);
+}
+
+}  // namespace qp

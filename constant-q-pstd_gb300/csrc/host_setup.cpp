@@ -10,6 +10,7 @@
 // negative-frequency shift phases.
 #include "host_setup.h"
 
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -133,14 +134,34 @@ static bool smooth7(int v) {
     return v == 1;
 }
 
+// Radices of the register passes (each 2..16): fewest passes first, then the
+// largest smallest radix, since a pass of radix R keeps m/R threads per line
+// busy (5184 -> 9,9,8,8 runs on 648 threads; 1728 -> 12,12,12 on 144).
+static void factor_search(int v, int maxr, std::vector<int>& cur, std::vector<int>& best) {
+    if (v == 1) {
+        if (best.empty() || cur.size() < best.size() ||
+            (cur.size() == best.size() && *std::min_element(cur.begin(), cur.end()) >
+                                              *std::min_element(best.begin(), best.end())))
+            best = cur;
+        return;
+    }
+    if (!best.empty() && cur.size() + 1 > best.size()) return;
+    for (int r = std::min(maxr, 16); r >= 2; r--) {
+        if (v % r) continue;
+        cur.push_back(r);
+        factor_search(v / r, r, cur, best);  // non-increasing radices: each multiset once
+        cur.pop_back();
+    }
+}
+
 static bool factor_direct(int n, std::vector<int>& rad) {
     rad.clear();
-    int v = n;
-    while (v % 4 == 0) { rad.push_back(4); v /= 4; }
-    while (v % 2 == 0) { rad.push_back(2); v /= 2; }
-    for (int f : {3, 5, 7, 11, 13})
-        while (v % f == 0) { rad.push_back(f); v /= f; }
-    return v == 1 && (int)rad.size() <= QP_MAXST;
+    if (n > 65535) return false;
+    std::vector<int> cur;
+    factor_search(n, 16, cur, rad);
+    if (rad.empty() || (int)rad.size() > QP_MAXST) return false;
+    const int rmin = *std::min_element(rad.begin(), rad.end());
+    return n / rmin <= QP_MAXTHREADS;
 }
 
 // Host Stockham in double (same recurrence as the device engine).
@@ -178,14 +199,28 @@ static void host_fft(std::vector<std::complex<double>>& x, const std::vector<int
 int build_plan_host(int n, HostPlan& hp) {
     hp.n = n;
     hp.blue = 0;
-    if (factor_direct(n, hp.rad)) {
+    if (n == 1) {
+        hp.m = 1;
+        hp.rad.clear();
+    } else if (factor_direct(n, hp.rad)) {
         hp.m = n;
     } else {
+        // Bluestein: the {2,3,5,7}-smooth inner length in [2n-1, 2.3n] with the
+        // lowest pass work, m * (passes + 1)
         hp.blue = 1;
-        int m = 2 * n - 1;
-        while (!smooth7(m)) m++;
-        hp.m = m;
-        if (!factor_direct(m, hp.rad)) return -1;
+        double best = 1e300;
+        for (int m = 2 * n - 1; m <= (int)(2.3 * n) + 8; m++) {
+            if (!smooth7(m)) continue;
+            std::vector<int> r;
+            if (!factor_direct(m, r)) continue;
+            const double cost = (double)m * (r.size() + 1);
+            if (cost < best) {
+                best = cost;
+                hp.m = m;
+                hp.rad = r;
+            }
+        }
+        if (best == 1e300) return -1;
     }
     const int m = hp.m;
     hp.w.resize(m);

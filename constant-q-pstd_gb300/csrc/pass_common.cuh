@@ -1,0 +1,60 @@
+// pass_common.cuh -- global<->shared movement shared by the pass kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "qpstd_internal.h"
+
+namespace qp {
+
+// Compensated accumulation s += v (Kahan), used for the image and the
+// illumination sums over thousands of steps.
+__device__ __forceinline__ void kahan_add(float* s, float* c, size_t i, float v) {
+    const float y = v - c[i];
+    const float t = s[i] + y;
+    c[i] = (t - s[i]) - y;
+    s[i] = t;
+}
+
+// z passes: this thread's line packs x rows r0 (re) and r1 (im).
+__device__ __forceinline__ void zload_pair(const float* __restrict__ f, float2* line, int nzz, bool has0, bool has1,
+                                           size_t r0, size_t r1) {
+    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+        float2 v;
+        v.x = has0 ? f[r0 + k] : 0.f;
+        v.y = has1 ? f[r1 + k] : 0.f;
+        line[k] = v;
+    }
+}
+
+// x passes: a CTA owns TZ = 2L consecutive z columns (TZ a power of two); line
+// l holds columns (iz0+2l, iz0+2l+1) in re/im, indexed by x.  Global accesses
+// walk (ix, c) with c fastest so each x row is read as one TZ-float segment.
+struct XTile {
+    int iz0, tzlog, tot, t0, nthr, nzz;
+    __device__ __forceinline__ XTile(int L, int bx, int nzz_, int nxx) {
+        const int TZ = 2 * L;
+        tzlog = 31 - __clz(TZ);
+        iz0 = bx * TZ;
+        tot = nxx * TZ;
+        t0 = threadIdx.y * blockDim.x + threadIdx.x;
+        nthr = blockDim.x * blockDim.y;
+        nzz = nzz_;
+    }
+    __device__ __forceinline__ void split(int g, int& c, int& ix) const {
+        c = g & ((1 << tzlog) - 1);
+        ix = g >> tzlog;
+    }
+    // float index of (column c, position ix) in the packed shared lines
+    __device__ __forceinline__ int sidx(int c, int ix, int ld) const { return 2 * ((c >> 1) * ld + ix) + (c & 1); }
+};
+
+__device__ __forceinline__ void xload(const float* __restrict__ f, float* sf, const XTile& T, int ld) {
+    for (int g = T.t0; g < T.tot; g += T.nthr) {
+        int c, ix;
+        T.split(g, c, ix);
+        const int iz = T.iz0 + c;
+        sf[T.sidx(c, ix, ld)] = (iz < T.nzz) ? f[(size_t)ix * T.nzz + iz] : 0.f;
+    }
+}
+
+}  // namespace qp

@@ -2,17 +2,30 @@
 #pragma once
 #include <cuda_runtime.h>
 
-#define QP_MAXST 24
+#define QP_MAXST 10
+// Threads per CTA of the pass kernels (__launch_bounds__(QP_MAXTHREADS, 1):
+// 80 registers per thread, enough for the radix-16 butterflies).
+#define QP_MAXTHREADS 768
 
 namespace qp {
+
+// One Stockham pass of a length-m transform.
+struct FFTPass {
+    int R;                 // radix (2..16)
+    int ns;                // product of the radices of the earlier passes
+    int B;                 // butterflies per line, m / R
+    int twstride;          // m / (ns * R): stride into the length-m twiddle table
+    unsigned ns_magic;     // ceil(2^32 / ns): j / ns = umulhi(j, ns_magic) for j < 2^16
+};
 
 // Device view of a line-FFT plan for one transform length n.
 struct FFTPlanDev {
     int n;                 // logical length (the grid size along the line)
     int m;                 // inner transform length (n, or the Bluestein length)
     int blue;              // 1 if Bluestein is used
-    int nst;               // number of Stockham stages of the length-m transform
-    int rad[QP_MAXST];     // radix of each stage
+    int nst;               // number of passes of the length-m transform
+    int tx;                // threads per line (>= max B, multiple of 32)
+    FFTPass pass[QP_MAXST];
     const float2* w;       // m twiddles e^{-2 pi i k/m}
     const float2* chirp;   // n chirp values e^{-i pi k^2/n} (Bluestein)
     const float2* bhat;    // m values: DFT_m of the wrapped conj chirp, divided by m (Bluestein)

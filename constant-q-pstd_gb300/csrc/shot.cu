@@ -61,7 +61,19 @@ static int upload_plan(qpstd_shot* s, const HostPlan& hp, FFTPlanDev& d) {
     d.m = hp.m;
     d.blue = hp.blue;
     d.nst = (int)hp.rad.size();
-    for (int i = 0; i < d.nst; i++) d.rad[i] = hp.rad[i];
+    int ns = 1, maxb = 1;
+    for (int i = 0; i < d.nst; i++) {
+        FFTPass& p = d.pass[i];
+        p.R = hp.rad[i];
+        p.ns = ns;
+        p.B = hp.m / p.R;
+        p.twstride = hp.m / (ns * p.R);
+        p.ns_magic = (ns > 1) ? (unsigned)(((1ull << 32) + ns - 1) / ns) : 0u;
+        maxb = std::max(maxb, p.B);
+        ns *= p.R;
+    }
+    d.tx = std::min(QP_MAXTHREADS, (maxb + 31) / 32 * 32);
+    if (maxb > QP_MAXTHREADS) return fail(QPSTD_ENOTSUP, "transform needs more threads per line than a CTA holds");
     const size_t cnt = hp.w.size() + hp.chirp.size() + hp.bhat.size();
     std::vector<float2> h(cnt);
     size_t o = 0;
@@ -78,11 +90,19 @@ static int upload_plan(qpstd_shot* s, const HostPlan& hp, FFTPlanDev& d) {
     return QPSTD_OK;
 }
 
-static int choose_pairs(int nlines, int m) {
-    const int pairs = (nlines + 1) / 2;
-    const int lmax = std::max(1, std::min(8, (96 * 1024) / (16 * m)));
-    int L = (pairs + 2 * 152 - 1) / (2 * 152);
-    return std::max(1, std::min(L, lmax));
+// Complex lines per CTA: bounded by the CTA's threads (tx per line), by shared
+// memory (nbuf line buffers of m float2), and small enough that the grid
+// covers the 152 SMs about twice.  pow2: x tiles need a power of two.
+static int choose_L(int nlines, int m, int tx, int nbuf, bool pow2) {
+    const int lmax = std::max(1, std::min(QP_MAXTHREADS / tx, (int)((160 * 1024) / ((size_t)8 * m * nbuf))));
+    int L = (nlines + 2 * 152 - 1) / (2 * 152);
+    L = std::max(1, std::min(L, lmax));
+    if (pow2) {
+        int p = 1;
+        while (p * 2 <= L) p *= 2;
+        L = p;
+    }
+    return L;
 }
 
 static int validate(const qpstd_shot_desc* d) {
@@ -315,13 +335,14 @@ extern "C" int qpstd_shot_create(const qpstd_shot_desc* d, qpstd_shot** out) {
         if (build_plan_host(nxx, hx) || build_plan_host(nzz, hz)) return bail(fail(QPSTD_ENOTSUP, "no FFT plan for this length"));
         if ((rc = upload_plan(s, hx, s->px))) return bail(rc);
         if ((rc = upload_plan(s, hz, s->pz))) return bail(rc);
-        s->Lx = choose_pairs(nzz, s->px.m);
-        s->Lzp = choose_pairs(nxx, s->pz.m);
-        // constant-Q passes hold three line buffers (z pass B, 3-output x-spectral pass)
-        s->Lzv = std::max(1, std::min(s->Lzp, (150 * 1024) / (24 * s->pz.m)));
-        s->Lxs = std::max(1, std::min(8, std::min((s->nzh + 151) / 152, (96 * 1024) / (16 * s->px.m))));
-        s->Lxs3 = std::max(1, std::min(s->Lxs, (150 * 1024) / (24 * s->px.m)));
-        if (24.0 * s->px.m > 200 * 1024 || 24.0 * s->pz.m > 200 * 1024)
+        const int pairs_z = (nxx + 1) / 2, pairs_x = (nzz + 1) / 2;
+        s->Lx = choose_L(pairs_x, s->px.m, s->px.tx, 1, true);
+        s->Lzp = choose_L(pairs_z, s->pz.m, s->pz.tx, 1, false);
+        // constant-Q: z pass B and the 3-output x-spectral pass hold two line buffers
+        s->Lzv = choose_L(pairs_z, s->pz.m, s->pz.tx, 2, false);
+        s->Lxs = choose_L(s->nzh, s->px.m, s->px.tx, 1, true);
+        s->Lxs3 = choose_L(s->nzh, s->px.m, s->px.tx, 2, true);
+        if (16.0 * s->px.m > 200 * 1024 || 16.0 * s->pz.m > 200 * 1024)
             return bail(fail(QPSTD_ENOTSUP, "line too long for one CTA"));
     }
     if (s->visco && (rc = setup_visco(s, d))) return bail(rc);

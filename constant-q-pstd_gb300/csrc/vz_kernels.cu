@@ -13,277 +13,223 @@
 // vz update), x pass (Px, vx update, next Dx; shared with the acoustic step),
 // x-spectral pass (aux symbol).  The aux spectrum is turned back into a real
 // field at the start of the next step's z pass A.
-#include "fftline.cuh"
+//
+// Half spectra: S[ix*nzh + kz], kz in [0, nzz/2].  Two real z-lines a, b are
+// transformed as one complex line z = a + ib; A(k) = (Z(k) + conj Z(n-k))/2,
+// B(k) = (Z(k) - conj Z(n-k))/(2i), and back Z(k) = A(k) + iB(k).
+#include "fft_reg.cuh"
+#include "pass_common.cuh"
 
 namespace qp {
 
-__device__ __forceinline__ void kahan_add2(float* s, float* c, size_t i, float v) {
-    const float y = v - c[i];
-    const float t = s[i] + y;
-    c[i] = (t - s[i]) - y;
-    s[i] = t;
-}
-
-// packed load of two real z-lines per complex line
-__device__ __forceinline__ void zload(const float* __restrict__ f, float2* dst, int L, int ld, int nxx, int nzz,
-                                      int ix0) {
-    const int tot = L * nzz;
-    for (int g = threadIdx.x; g < tot; g += blockDim.x) {
-        const int l = g / nzz, k = g - l * nzz;
-        const int xa = ix0 + 2 * l;
-        float2 v;
-        v.x = (xa < nxx) ? f[(size_t)xa * nzz + k] : 0.f;
-        v.y = (xa + 1 < nxx) ? f[(size_t)(xa + 1) * nzz + k] : 0.f;
-        dst[l * ld + k] = v;
-    }
-    __syncthreads();
-}
-
-// Full packed spectrum Z = A + iB of lines (xa, xa+1) from their half spectra.
-__device__ __forceinline__ void zrepack(const float2* __restrict__ S, float2* dst, int L, int ld, int nxx, int nzz,
-                                        int nzh, int ix0) {
-    const int tot = L * nzz;
-    for (int g = threadIdx.x; g < tot; g += blockDim.x) {
-        const int l = g / nzz, k = g - l * nzz;
-        const int xa = ix0 + 2 * l;
+// this thread's packed line <- half spectra of rows (xa, xa+1)
+__device__ __forceinline__ void zrepack(const float2* __restrict__ S, float2* line, int nzz, int nzh, bool has0,
+                                        bool has1, int xa) {
+    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const int kk = (k < nzh) ? k : nzz - k;
-        float2 A = make_float2(0.f, 0.f), B = make_float2(0.f, 0.f);
-        if (xa < nxx) A = S[(size_t)xa * nzh + kk];
-        if (xa + 1 < nxx) B = S[(size_t)(xa + 1) * nzh + kk];
-        float2 z;
-        if (k < nzh) z = make_float2(A.x - B.y, A.y + B.x);
-        else z = make_float2(A.x + B.y, -A.y + B.x);
-        dst[l * ld + k] = z;
+        const float2 A = has0 ? S[(size_t)xa * nzh + kk] : make_float2(0.f, 0.f);
+        const float2 B = has1 ? S[(size_t)(xa + 1) * nzh + kk] : make_float2(0.f, 0.f);
+        line[k] = (k < nzh) ? make_float2(A.x - B.y, A.y + B.x) : make_float2(A.x + B.y, -A.y + B.x);
     }
-    __syncthreads();
 }
 
-// Split a packed forward spectrum into the half spectra of its two lines.
-__device__ __forceinline__ void zunpack(const float2* r, float2* __restrict__ S, int L, int ld, int nxx, int nzz,
-                                        int nzh, int ix0) {
-    const int tot = L * nzh;
-    for (int g = threadIdx.x; g < tot; g += blockDim.x) {
-        const int l = g / nzh, k = g - l * nzh;
-        const int xa = ix0 + 2 * l;
-        const float2 z = r[l * ld + k];
-        const float2 w = r[l * ld + ((k == 0) ? 0 : nzz - k)];
-        if (xa < nxx) S[(size_t)xa * nzh + k] = make_float2(0.5f * (z.x + w.x), 0.5f * (z.y - w.y));
-        if (xa + 1 < nxx) S[(size_t)(xa + 1) * nzh + k] = make_float2(0.5f * (z.y + w.y), -0.5f * (z.x - w.x));
+// half spectra of rows (xa, xa+1) <- this thread's transformed packed line
+__device__ __forceinline__ void zunpack(const float2* line, float2* __restrict__ S, int nzz, int nzh, bool has0,
+                                        bool has1, int xa) {
+    for (int k = threadIdx.x; k < nzh; k += blockDim.x) {
+        const float2 z = line[k];
+        const float2 w = line[(k == 0) ? 0 : nzz - k];
+        if (has0) S[(size_t)xa * nzh + k] = make_float2(0.5f * (z.x + w.x), 0.5f * (z.y - w.y));
+        if (has1) S[(size_t)(xa + 1) * nzh + k] = make_float2(0.5f * (z.y + w.y), -0.5f * (z.x - w.x));
     }
 }
+
+#define ZPASS_SETUP                                                  \
+    extern __shared__ float2 smem[];                                 \
+    __shared__ FFTPass s_pass[QP_MAXST];                             \
+    const FFTCtx fc = make_ctx(a.pl, s_pass);                        \
+    const int L = a.L, ld = a.pl.m, nzz = a.nzz, nxx = a.nxx;        \
+    float2* line = smem + threadIdx.y * ld;                          \
+    const int xa = blockIdx.x * 2 * L + 2 * threadIdx.y;             \
+    const bool has0 = xa < nxx, has1 = xa + 1 < nxx;                 \
+    const size_t r0 = (size_t)xa * nzz, r1 = r0 + nzz;               \
+    (void)r1;
 
 // ---- z pass A ---------------------------------------------------------------
-__global__ void __launch_bounds__(256) vz_passA_kernel(VzArgsA a) {
-    extern __shared__ float2 smem[];
-    const int L = a.L, ld = a.pl.m, nzz = a.nzz, nxx = a.nxx, nzh = a.nzh;
-    float2* b0 = smem;
-    float2* b1 = smem + L * ld;
-    const int ix0 = blockIdx.x * 2 * L;
-    const int tot = L * nzz;
+__global__ void __launch_bounds__(768, 1) vz_passA_kernel(VzArgsA a) {
+    ZPASS_SETUP
+    const int nzh = a.nzh;
     if (a.aux_spec) {
-        zrepack(a.aux_spec, b0, L, ld, nxx, nzz, nzh, ix0);
-        float2* r = dft_lines(b0, b1, L, ld, a.pl, +1.f);
-        for (int g = threadIdx.x; g < tot; g += blockDim.x) {
-            const int l = g / nzz, k = g - l * nzz;
-            const int xa = ix0 + 2 * l;
-            const float2 v = r[l * ld + k];
-            if (xa < nxx) a.aux[(size_t)xa * nzz + k] = v.x;
-            if (xa + 1 < nxx) a.aux[(size_t)(xa + 1) * nzz + k] = v.y;
+        zrepack(a.aux_spec, line, nzz, nzh, has0, has1, xa);
+        __syncthreads();
+        dft_n<+1>(smem, ld, fc, L);
+        for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+            const float2 v = line[k];
+            if (has0) a.aux[r0 + k] = v.x;
+            if (has1) a.aux[r1 + k] = v.y;
         }
         __syncthreads();
     }
-    zload(a.vz, b0, L, ld, nxx, nzz, ix0);
-    float2* r = roundtrip_c(b0, b1, L, ld, a.pl, a.HzM);
-    float2* o = (r == b0) ? b1 : b0;
-    for (int g = threadIdx.x; g < tot; g += blockDim.x) {
-        const int l = g / nzz, k = g - l * nzz;
-        const int xa = ix0 + 2 * l;
-        const float2 d = r[l * ld + k];
+    zload_pair(a.vz, line, nzz, has0, has1, r0, r1);
+    __syncthreads();
+    roundtrip_c(smem, ld, fc, L, a.HzM);
+    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+        const float2 d = line[k];
         const float ib = a.i_bz[k], ia = a.i_az[k];
         float2 dv = make_float2(0.f, 0.f);
-        if (xa < nxx) {
-            const size_t i = (size_t)xa * nzz + k;
-            const float ps = ib * a.psi_vz[i] + ia * d.x;
-            a.psi_vz[i] = ps;
-            dv.x = a.Dx[i] + (d.x + ps);
-            a.div[i] = dv.x;
+        if (has0) {
+            const float ps = ib * a.psi_vz[r0 + k] + ia * d.x;
+            a.psi_vz[r0 + k] = ps;
+            dv.x = a.Dx[r0 + k] + (d.x + ps);
+            a.div[r0 + k] = dv.x;
         }
-        if (xa + 1 < nxx) {
-            const size_t i = (size_t)(xa + 1) * nzz + k;
-            const float ps = ib * a.psi_vz[i] + ia * d.y;
-            a.psi_vz[i] = ps;
-            dv.y = a.Dx[i] + (d.y + ps);
-            a.div[i] = dv.y;
+        if (has1) {
+            const float ps = ib * a.psi_vz[r1 + k] + ia * d.y;
+            a.psi_vz[r1 + k] = ps;
+            dv.y = a.Dx[r1 + k] + (d.y + ps);
+            a.div[r1 + k] = dv.y;
         }
-        o[l * ld + k] = dv;
+        line[k] = dv;
     }
     __syncthreads();
-    float2* oth = (o == b0) ? b1 : b0;
-    r = dft_lines(o, oth, L, ld, a.pl, -1.f);
-    zunpack(r, a.G, L, ld, nxx, nzz, nzh, ix0);
+    dft_n<-1>(smem, ld, fc, L);
+    zunpack(line, a.G, nzz, nzh, has0, has1, xa);
 }
 
 // ---- x-spectral pass ----------------------------------------------------------
-__global__ void __launch_bounds__(256) vz_xspec_kernel(VxsArgs a) {
+// L kz columns per CTA (L a power of two); line c = column kz0 + c.
+__device__ __forceinline__ float spec_symbol(const VxsArgs& a, int j, float k2) {
+    if (a.mode == 0) {
+        if (j == 1) return k2;
+        const float k32 = exp2f(log2f(k2) * (1.f / 32.f));
+        return (j == 0) ? k32 : k2 * k32;
+    }
+    const float ka = exp2f(0.505f * log2f(k2));
+    if (a.mode == 1) return ka;
+    const float num = 2.f * a.eta6 * ka * (1.f + a.tao * a.dt * ka);
+    const float den = expf(-a.tao * a.tt * ka) + a.eta6 * expf(a.tao * a.dt * ka);
+    return ka - num / den;
+}
+
+__global__ void __launch_bounds__(768, 1) vz_xspec_kernel(VxsArgs a) {
     extern __shared__ float2 smem[];
+    __shared__ FFTPass s_pass[QP_MAXST];
+    const FFTCtx fc = make_ctx(a.pl, s_pass);
     const int L = a.L, ld = a.pl.m, nxx = a.nxx, nzh = a.nzh;
-    float2* b0 = smem;
-    float2* b1 = smem + L * ld;
-    float2* b2 = smem + 2 * L * ld;  // mode 0 keeps the forward spectrum here
+    const int lg = 31 - __clz(L);
     const int kz0 = blockIdx.x * L;
+    const int t0 = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
     const int tot = L * nxx;
-    for (int g = threadIdx.x; g < tot; g += blockDim.x) {
-        const int c = g % L, ix = g / L;
+    const int nout = (a.mode == 0) ? 3 : 1;
+    float2* X = smem + (size_t)L * ld;  // kept forward spectrum (three-output mode)
+    float2* line = smem + threadIdx.y * ld;
+    for (int g = t0; g < tot; g += nthr) {
+        const int c = g & (L - 1), ix = g >> lg;
         const int kz = kz0 + c;
-        b0[c * ld + ix] = (kz < nzh) ? a.in[(size_t)ix * nzh + kz] : make_float2(0.f, 0.f);
+        smem[c * ld + ix] = (kz < nzh) ? a.in[(size_t)ix * nzh + kz] : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    float2* X = dft_lines(b0, b1, L, ld, a.pl, -1.f);
-    const int nout = (a.mode == 0) ? 3 : 1;
-    if (nout == 3 && X != b2) {
-        for (int g = threadIdx.x; g < tot; g += blockDim.x) {
-            const int c = g / nxx, ix = g - c * nxx;
-            b2[c * ld + ix] = X[c * ld + ix];
-        }
+    dft_n<-1>(smem, ld, fc, L);
+    const int kz = kz0 + threadIdx.y;
+    const float kzsq = a.kz2[(kz < nzh) ? kz : 0];
+    if (nout == 3) {
+        for (int ix = threadIdx.x; ix < nxx; ix += blockDim.x) X[threadIdx.y * ld + ix] = line[ix];
         __syncthreads();
-        X = b2;
     }
     for (int j = 0; j < nout; j++) {
-        // three outputs: X stays in b2 and each output ping-pongs in b0/b1;
-        // one output: the product goes to the free buffer, X's buffer is scratch
-        float2* y = (nout == 3) ? b0 : ((X == b0) ? b1 : b0);
-        float2* z = (nout == 3) ? b1 : X;
-        for (int g = threadIdx.x; g < tot; g += blockDim.x) {
-            const int c = g / nxx, ix = g - c * nxx;
-            const int kz = kz0 + c;
-            const float k2 = a.kx2[ix] + a.kz2[(kz < nzh) ? kz : 0];
-            float sym;
-            if (a.mode == 0) {
-                if (j == 1) {
-                    sym = k2;
-                } else {
-                    const float lk = log2f(k2);
-                    const float k32 = exp2f(lk * (1.f / 32.f));
-                    sym = (j == 0) ? k32 : k2 * k32;
-                }
-            } else {
-                const float ka = exp2f(0.505f * log2f(k2));
-                if (a.mode == 1) {
-                    sym = ka;
-                } else {
-                    const float num = 2.f * a.eta6 * ka * (1.f + a.tao * a.dt * ka);
-                    const float den = expf(-a.tao * a.tt * ka) + a.eta6 * expf(a.tao * a.dt * ka);
-                    sym = ka - num / den;
-                }
-            }
-            y[c * ld + ix] = cscale(X[c * ld + ix], sym * a.norm);
-        }
+        const float2* src = (nout == 3) ? X + threadIdx.y * ld : line;
+        for (int ix = threadIdx.x; ix < nxx; ix += blockDim.x)
+            line[ix] = cscale(src[ix], spec_symbol(a, j, a.kx2[ix] + kzsq) * a.norm);
         __syncthreads();
-        float2* r = dft_lines(y, z, L, ld, a.pl, +1.f);
+        dft_n<+1>(smem, ld, fc, L);
         float2* out = (j == 0) ? a.out0 : ((j == 1) ? a.out1 : a.out2);
-        for (int g = threadIdx.x; g < tot; g += blockDim.x) {
-            const int c = g % L, ix = g / L;
-            const int kz = kz0 + c;
-            if (kz < nzh) out[(size_t)ix * nzh + kz] = r[c * ld + ix];
+        for (int g = t0; g < tot; g += nthr) {
+            const int c = g & (L - 1), ix = g >> lg;
+            if (kz0 + c < nzh) out[(size_t)ix * nzh + kz0 + c] = smem[c * ld + ix];
         }
         __syncthreads();
     }
 }
 
 // ---- z pass B -----------------------------------------------------------------
-__global__ void __launch_bounds__(256) vz_passB_kernel(VzArgsB a) {
-    extern __shared__ float2 smem[];
-    const int L = a.L, ld = a.pl.m, nzz = a.nzz, nxx = a.nxx, nzh = a.nzh;
-    float2* b0 = smem;
-    float2* b1 = smem + L * ld;
-    float2* acc = smem + 2 * L * ld;  // running total (packed pairs)
-    const int ix0 = blockIdx.x * 2 * L;
-    const int tot = L * nzz;
-    const float2* specs[3] = {a.Y2, a.Y3, a.Y4};
+__global__ void __launch_bounds__(768, 1) vz_passB_kernel(VzArgsB a) {
+    ZPASS_SETUP
+    const int nzh = a.nzh;
+    float2* acc = smem + (size_t)(L + threadIdx.y) * ld;  // running total of this line pair
     for (int j = 0; j < 3; j++) {
-        zrepack(specs[j], b0, L, ld, nxx, nzz, nzh, ix0);
-        float2* r = dft_lines(b0, b1, L, ld, a.pl, +1.f);
-        for (int g = threadIdx.x; g < tot; g += blockDim.x) {
-            const int l = g / nzz, k = g - l * nzz;
-            const int xa = ix0 + 2 * l;
-            const float2 y = r[l * ld + k];
-            float2 t = (j == 0) ? make_float2(0.f, 0.f) : acc[l * ld + k];
-            const float* cf = (j == 0) ? a.y2 : ((j == 1) ? a.y3c : a.y4c);
-            const float sg = (j == 0) ? 1.f : -1.f;
-            if (xa < nxx) t.x += sg * cf[(size_t)xa * nzz + k] * y.x;
-            if (xa + 1 < nxx) t.y += sg * cf[(size_t)(xa + 1) * nzz + k] * y.y;
-            acc[l * ld + k] = t;
+        const float2* spec = (j == 0) ? a.Y2 : ((j == 1) ? a.Y3 : a.Y4);
+        const float* cf = (j == 0) ? a.y2 : ((j == 1) ? a.y3c : a.y4c);
+        const float sg = (j == 0) ? 1.f : -1.f;
+        zrepack(spec, line, nzz, nzh, has0, has1, xa);
+        __syncthreads();
+        dft_n<+1>(smem, ld, fc, L);
+        for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+            const float2 y = line[k];
+            float2 t = (j == 0) ? make_float2(0.f, 0.f) : acc[k];
+            if (has0) t.x += sg * cf[r0 + k] * y.x;
+            if (has1) t.y += sg * cf[r1 + k] * y.y;
+            acc[k] = t;
         }
         __syncthreads();
     }
-    for (int g = threadIdx.x; g < tot; g += blockDim.x) {
-        const int l = g / nzz, k = g - l * nzz;
-        const int xa = ix0 + 2 * l;
-        float2 t = acc[l * ld + k];
+    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+        const float2 t = acc[k];
         float2 v = make_float2(0.f, 0.f);
-        if (xa < nxx) {
-            const size_t i = (size_t)xa * nzz + k;
-            v.x = a.y1[i] * a.div[i] + t.x;
-            a.total[i] = v.x;
+        if (has0) {
+            v.x = a.y1[r0 + k] * a.div[r0 + k] + t.x;
+            a.total[r0 + k] = v.x;
         }
-        if (xa + 1 < nxx) {
-            const size_t i = (size_t)(xa + 1) * nzz + k;
-            v.y = a.y1[i] * a.div[i] + t.y;
-            a.total[i] = v.y;
+        if (has1) {
+            v.y = a.y1[r1 + k] * a.div[r1 + k] + t.y;
+            a.total[r1 + k] = v.y;
         }
-        b0[l * ld + k] = v;
+        line[k] = v;
     }
     __syncthreads();
-    float2* r = dft_lines(b0, b1, L, ld, a.pl, -1.f);
-    zunpack(r, a.T, L, ld, nxx, nzz, nzh, ix0);
+    dft_n<-1>(smem, ld, fc, L);
+    zunpack(line, a.T, nzz, nzh, has0, has1, xa);
 }
 
 // ---- z pass C -----------------------------------------------------------------
-__global__ void __launch_bounds__(256) vz_passC_kernel(VzArgsC a) {
-    extern __shared__ float2 smem[];
-    const int L = a.L, ld = a.pl.m, nzz = a.nzz, nxx = a.nxx, nzh = a.nzh;
-    float2* b0 = smem;
-    float2* b1 = smem + L * ld;
-    const int ix0 = blockIdx.x * 2 * L;
-    const int tot = L * nzz;
-    zrepack(a.Dspec, b0, L, ld, nxx, nzz, nzh, ix0);
-    float2* r = dft_lines(b0, b1, L, ld, a.pl, +1.f);
-    float2* o = (r == b0) ? b1 : b0;
-    for (int g = threadIdx.x; g < tot; g += blockDim.x) {
-        const int l = g / nzz, k = g - l * nzz;
-        const int xa = ix0 + 2 * l;
-        const float2 D = r[l * ld + k];
+__global__ void __launch_bounds__(768, 1) vz_passC_kernel(VzArgsC a) {
+    ZPASS_SETUP
+    const int nzh = a.nzh;
+    zrepack(a.Dspec, line, nzz, nzh, has0, has1, xa);
+    __syncthreads();
+    dft_n<+1>(smem, ld, fc, L);
+    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+        const float2 D = line[k];
         float2 pn = make_float2(0.f, 0.f);
-        if (xa < nxx) {
-            const size_t i = (size_t)xa * nzz + k;
+        if (has0) {
+            const size_t i = r0 + k;
             pn.x = a.p[i] + a.e1[i] * (a.total[i] + a.sgn * a.e2[i] * D.x) + a.sgn * a.e3[i] * a.aux[i];
             if (xa == a.xs && k == a.zs) pn.x += a.src;
         }
-        if (xa + 1 < nxx) {
-            const size_t i = (size_t)(xa + 1) * nzz + k;
+        if (has1) {
+            const size_t i = r1 + k;
             pn.y = a.p[i] + a.e1[i] * (a.total[i] + a.sgn * a.e2[i] * D.y) + a.sgn * a.e3[i] * a.aux[i];
             if (xa + 1 == a.xs && k == a.zs) pn.y += a.src;
         }
-        o[l * ld + k] = pn;
+        line[k] = pn;
     }
     __syncthreads();
+    const int ix0 = blockIdx.x * 2 * L;
     if (a.rec_off) {
-        float* of = reinterpret_cast<float*>(o);
-        const int r0 = a.rec_off[blockIdx.x], r1 = a.rec_off[blockIdx.x + 1];
-        for (int q = r0 + threadIdx.x; q < r1; q += blockDim.x) {
+        float* sf = reinterpret_cast<float*>(smem);
+        const int t0 = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+        const int q0 = a.rec_off[blockIdx.x], q1 = a.rec_off[blockIdx.x + 1];
+        for (int q = q0 + t0; q < q1; q += nthr) {
             const RecEntry e = a.rec[q];
             const int rel = e.gx - ix0;
-            const size_t si = 2 * ((size_t)(rel >> 1) * ld + e.gz) + (rel & 1);
-            if (a.gather_row) a.gather_row[e.ir] = of[si];
-            if (a.obs_row && e.inject) of[si] = a.obs_row[e.ir];
+            const int si = 2 * ((rel >> 1) * ld + e.gz) + (rel & 1);
+            if (a.gather_row) a.gather_row[e.ir] = sf[si];
+            if (a.obs_row && e.inject) sf[si] = a.obs_row[e.ir];
         }
         __syncthreads();
     }
     const int pml = a.pml, nz = nzz - 2 * pml;
-    for (int g = threadIdx.x; g < tot; g += blockDim.x) {
-        const int l = g / nzz, k = g - l * nzz;
-        const int xa = ix0 + 2 * l;
-        const float2 pn = o[l * ld + k];
+    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+        const float2 pn = line[k];
         for (int h = 0; h < 2; h++) {
             const int ix = xa + h;
             if (ix >= nxx) break;
@@ -292,37 +238,31 @@ __global__ void __launch_bounds__(256) vz_passC_kernel(VzArgsC a) {
             a.p[i] = v;
             if (ix >= pml && ix < nxx - pml && k >= pml && k < nzz - pml) {
                 const size_t j = (size_t)(ix - pml) * nz + (k - pml);
-                if (a.ssg) kahan_add2(a.ssg, a.ssg_c, j, v * v);
-                if (a.img) kahan_add2(a.img, a.img_c, j, a.ps[i] * v);
+                if (a.ssg) kahan_add(a.ssg, a.ssg_c, j, v * v);
+                if (a.img) kahan_add(a.img, a.img_c, j, a.ps[i] * v);
             }
         }
     }
+    __syncthreads();
     // forward z transform of the new p: half spectrum for the aux operator and
     // the staggered z derivative from the same transform
-    float2* oth = (o == b0) ? b1 : b0;
-    float2* X = dft_lines(o, oth, L, ld, a.pl, -1.f);
-    zunpack(X, a.P, L, ld, nxx, nzz, nzh, ix0);
+    dft_n<-1>(smem, ld, fc, L);
+    zunpack(line, a.P, nzz, nzh, has0, has1, xa);
     __syncthreads();
-    for (int g = threadIdx.x; g < tot; g += blockDim.x) {
-        const int l = g / nzz, k = g - l * nzz;
-        X[l * ld + k] = cmul(X[l * ld + k], __ldg(&a.HzP[k]));
-    }
+    for (int k = threadIdx.x; k < nzz; k += blockDim.x) line[k] = cmul(line[k], __ldg(&a.HzP[k]));
     __syncthreads();
-    oth = (X == b0) ? b1 : b0;
-    r = dft_lines(X, oth, L, ld, a.pl, +1.f);
-    for (int g = threadIdx.x; g < tot; g += blockDim.x) {
-        const int l = g / nzz, k = g - l * nzz;
-        const int xa = ix0 + 2 * l;
-        const float2 d = r[l * ld + k];
+    dft_n<+1>(smem, ld, fc, L);
+    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+        const float2 d = line[k];
         const float hb = a.h_bz[k], ha = a.h_az[k];
-        if (xa < nxx) {
-            const size_t i = (size_t)xa * nzz + k;
+        if (has0) {
+            const size_t i = r0 + k;
             const float ps = hb * a.psi_pz[i] + ha * d.x;
             a.psi_pz[i] = ps;
             a.vz[i] = a.vz[i] + a.dt * a.bbz[i] * (d.x + ps);
         }
-        if (xa + 1 < nxx) {
-            const size_t i = (size_t)(xa + 1) * nzz + k;
+        if (has1) {
+            const size_t i = r1 + k;
             const float ps = hb * a.psi_pz[i] + ha * d.y;
             a.psi_pz[i] = ps;
             a.vz[i] = a.vz[i] + a.dt * a.bbz[i] * (d.y + ps);
@@ -331,40 +271,36 @@ __global__ void __launch_bounds__(256) vz_passC_kernel(VzArgsC a) {
 }
 
 // ---- z inverse only -------------------------------------------------------------
-__global__ void __launch_bounds__(256) vz_zinv_kernel(VzArgsI a) {
-    extern __shared__ float2 smem[];
-    const int L = a.L, ld = a.pl.m, nzz = a.nzz, nxx = a.nxx;
-    float2* b0 = smem;
-    float2* b1 = smem + L * ld;
-    const int ix0 = blockIdx.x * 2 * L;
-    zrepack(a.spec, b0, L, ld, nxx, nzz, a.nzh, ix0);
-    float2* r = dft_lines(b0, b1, L, ld, a.pl, +1.f);
-    for (int g = threadIdx.x; g < L * nzz; g += blockDim.x) {
-        const int l = g / nzz, k = g - l * nzz;
-        const int xa = ix0 + 2 * l;
-        const float2 v = r[l * ld + k];
-        if (xa < nxx) a.out[(size_t)xa * nzz + k] = v.x;
-        if (xa + 1 < nxx) a.out[(size_t)(xa + 1) * nzz + k] = v.y;
+__global__ void __launch_bounds__(768, 1) vz_zinv_kernel(VzArgsI a) {
+    ZPASS_SETUP
+    zrepack(a.spec, line, nzz, a.nzh, has0, has1, xa);
+    __syncthreads();
+    dft_n<+1>(smem, ld, fc, L);
+    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+        const float2 v = line[k];
+        if (has0) a.out[r0 + k] = v.x;
+        if (has1) a.out[r1 + k] = v.y;
     }
 }
 
 // ---- launchers -------------------------------------------------------------------
-static size_t zsm(int L, int m, int nbuf) { return sizeof(float2) * (size_t)nbuf * L * m; }
+static size_t lsm(int L, int m, int nbuf) { return sizeof(float2) * (size_t)nbuf * L * m; }
+static int zgrid(int nxx, int L) { return (nxx + 2 * L - 1) / (2 * L); }
 
 void launch_vz_passA(const VzArgsA& a, cudaStream_t s) {
-    vz_passA_kernel<<<(a.nxx + 2 * a.L - 1) / (2 * a.L), 256, zsm(a.L, a.pl.m, 2), s>>>(a);
+    vz_passA_kernel<<<zgrid(a.nxx, a.L), dim3(a.pl.tx, a.L), lsm(a.L, a.pl.m, 1), s>>>(a);
 }
 void launch_vz_xspec(const VxsArgs& a, cudaStream_t s) {
-    vz_xspec_kernel<<<(a.nzh + a.L - 1) / a.L, 256, zsm(a.L, a.pl.m, a.mode == 0 ? 3 : 2), s>>>(a);
+    vz_xspec_kernel<<<(a.nzh + a.L - 1) / a.L, dim3(a.pl.tx, a.L), lsm(a.L, a.pl.m, a.mode == 0 ? 2 : 1), s>>>(a);
 }
 void launch_vz_passB(const VzArgsB& a, cudaStream_t s) {
-    vz_passB_kernel<<<(a.nxx + 2 * a.L - 1) / (2 * a.L), 256, zsm(a.L, a.pl.m, 3), s>>>(a);
+    vz_passB_kernel<<<zgrid(a.nxx, a.L), dim3(a.pl.tx, a.L), lsm(a.L, a.pl.m, 2), s>>>(a);
 }
 void launch_vz_passC(const VzArgsC& a, cudaStream_t s) {
-    vz_passC_kernel<<<(a.nxx + 2 * a.L - 1) / (2 * a.L), 256, zsm(a.L, a.pl.m, 2), s>>>(a);
+    vz_passC_kernel<<<zgrid(a.nxx, a.L), dim3(a.pl.tx, a.L), lsm(a.L, a.pl.m, 1), s>>>(a);
 }
 void launch_vz_zinv(const VzArgsI& a, cudaStream_t s) {
-    vz_zinv_kernel<<<(a.nxx + 2 * a.L - 1) / (2 * a.L), 256, zsm(a.L, a.pl.m, 2), s>>>(a);
+    vz_zinv_kernel<<<zgrid(a.nxx, a.L), dim3(a.pl.tx, a.L), lsm(a.L, a.pl.m, 1), s>>>(a);
 }
 
 int vz_set_smem_limits() {
