@@ -155,66 +155,74 @@ template <int R, int S> __device__ __forceinline__ void dft(float2 (&v)[R]) {
 
 // ---- one Stockham pass over the lines of the CTA (in place) ------------------------
 // Thread (threadIdx.x, threadIdx.y) handles butterfly j = threadIdx.x of line
-// threadIdx.y.  Ends with a barrier.
-template <int R, int S>
-__device__ __noinline__ void reg_pass(float2* buf, int ld, const FFTPass ps, const float2* __restrict__ tw,
+// threadIdx.y.  The radix is a runtime value; all radices share one 16-entry
+// register array (constant indices under full unrolling), so one copy of the
+// pass serves every plan without register spills.  Ends with a barrier.
+template <int R> __device__ __forceinline__ float2 (&head(float2 (&v)[16]))[R] {
+    return *reinterpret_cast<float2(*)[R]>(&v[0]);
+}
+
+template <int S>
+__device__ __forceinline__ void reg_pass(float2* buf, int ld, const FFTPass& ps, const float2* __restrict__ tw,
                                          int L) {
+    const int R = ps.R;
     const int j = threadIdx.x;
     const int l = threadIdx.y;
     const bool act = (j < ps.B) && (l < L);
-    float2 v[R];
+    float2 v[16];
     int k = 0;
     float2* line = buf + l * ld;
     if (act) {
         k = (ps.ns == 1) ? 0 : (int)(j - __umulhi((unsigned)j, ps.ns_magic) * ps.ns);
 #pragma unroll
-        for (int r = 0; r < R; r++) v[r] = line[j + r * ps.B];
+        for (int r = 0; r < 16; r++)
+            if (r < R) v[r] = line[j + r * ps.B];
         if (ps.ns > 1) {
             float2 w1 = __ldg(&tw[k * ps.twstride]);
             if (S > 0) w1.y = -w1.y;
             float2 w = w1;
 #pragma unroll
-            for (int r = 1; r < R; r++) {
-                v[r] = cmul(v[r], w);
-                if (r + 1 < R) w = cmul(w, w1);
-            }
+            for (int r = 1; r < 16; r++)
+                if (r < R) {
+                    v[r] = cmul(v[r], w);
+                    w = cmul(w, w1);
+                }
         }
-        dft<R, S>(v);
+        switch (R) {
+            case 2: dft<2, S>(head<2>(v)); break;
+            case 3: dft<3, S>(head<3>(v)); break;
+            case 4: dft<4, S>(head<4>(v)); break;
+            case 5: dft<5, S>(head<5>(v)); break;
+            case 6: dft<6, S>(head<6>(v)); break;
+            case 7: dft<7, S>(head<7>(v)); break;
+            case 8: dft<8, S>(head<8>(v)); break;
+            case 9: dft<9, S>(head<9>(v)); break;
+            case 10: dft<10, S>(head<10>(v)); break;
+            case 11: dft<11, S>(head<11>(v)); break;
+            case 12: dft<12, S>(head<12>(v)); break;
+            case 13: dft<13, S>(head<13>(v)); break;
+            case 14: dft<14, S>(head<14>(v)); break;
+            case 15: dft<15, S>(head<15>(v)); break;
+            default: dft<16, S>(head<16>(v)); break;
+        }
     }
     __syncthreads();
     if (act) {
         const int base = (j - k) * R + k;
 #pragma unroll
-        for (int r = 0; r < R; r++) line[base + r * ps.ns] = v[r];
+        for (int r = 0; r < 16; r++)
+            if (r < R) line[base + r * ps.ns] = v[r];
     }
     __syncthreads();
 }
 
-// Length-m transform (unnormalised) of the L lines, in place.  One call per
-// transform: the pass loop and its radix switch live in this function, so the
-// kernels that use it hold a single copy of every radix.
+// Length-m transform (unnormalised) of the L lines, in place.
 template <int S>
 __device__ __forceinline__ void fft_m_impl(float2* buf, int ld, const FFTPass* __restrict__ sp, int nst,
-                                        const float2* __restrict__ tw, int L) {
+                                           const float2* __restrict__ tw, int L) {
     for (int i = 0; i < nst; i++) {
         const FFTPass ps = sp[i];
-        switch (ps.R) {
-            case 2: reg_pass<2, S>(buf, ld, ps, tw, L); break;
-            case 3: reg_pass<3, S>(buf, ld, ps, tw, L); break;
-            case 4: reg_pass<4, S>(buf, ld, ps, tw, L); break;
-            case 5: reg_pass<5, S>(buf, ld, ps, tw, L); break;
-            case 6: reg_pass<6, S>(buf, ld, ps, tw, L); break;
-            case 7: reg_pass<7, S>(buf, ld, ps, tw, L); break;
-            case 8: reg_pass<8, S>(buf, ld, ps, tw, L); break;
-            case 9: reg_pass<9, S>(buf, ld, ps, tw, L); break;
-            case 10: reg_pass<10, S>(buf, ld, ps, tw, L); break;
-            case 11: reg_pass<11, S>(buf, ld, ps, tw, L); break;
-            case 12: reg_pass<12, S>(buf, ld, ps, tw, L); break;
-            case 13: reg_pass<13, S>(buf, ld, ps, tw, L); break;
-            case 14: reg_pass<14, S>(buf, ld, ps, tw, L); break;
-            case 15: reg_pass<15, S>(buf, ld, ps, tw, L); break;
-            default: reg_pass<16, S>(buf, ld, ps, tw, L); break;
-        }
+        reg_pass<S>(buf, ld, ps, tw, L);
     }
 }
 

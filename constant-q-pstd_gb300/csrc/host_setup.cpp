@@ -90,7 +90,7 @@ static std::complex<double> ref_symbol(double a, double b, int i, int n) {
     return (i < n / 2 + 1) ? std::complex<double>(-b, a) : std::complex<double>(b, -a);
 }
 
-void shift_symbols(int n, double d, int which, std::vector<std::complex<double>>& H) {
+void shift_symbols(int n, double d, int which, std::vector<std::complex<double>>& H, bool raw) {
     // which: 0 = "m" tables used for the velocity derivative along x
     //            (kxsmr, kxsmi) ; 1 = "c" tables used for the pressure
     //            derivative along x (kxscr, kxsci) ; 2 = z velocity derivative
@@ -113,6 +113,12 @@ void shift_symbols(int n, double d, int which, std::vector<std::complex<double>>
             case 2: a[i] = k * sr[i]; b[i] = -k * si[i]; break;  // kzscr, kzsci
             default: a[i] = k * sr[i]; b[i] = k * si[i]; break;  // kzsmr, kzsmi
         }
+    }
+    if (raw) {
+        // the reference's own symbol, as multiplied inside its 2-D C2C path
+        H.assign(n, 0.0);
+        for (int i = 0; i < n; i++) H[i] = ref_symbol(a[i], b[i], i, n);
+        return;
     }
     // The reference keeps Re of a C2C inverse of real data, i.e. it applies the
     // Hermitian part (H(k) + conj(H(-k)))/2 of its symbol.  For odd n the

@@ -13,10 +13,11 @@ void pml_coeffs(int pml, double fm, int nxx, int nzz, double dx, double dz, doub
 // |k| on an n-point grid as the reference builds it (kkx / kkz).
 double wavenumber(int i, int n, double d);
 
-// Effective (Hermitian) staggered-derivative symbol divided by n.
+// Effective (Hermitian) staggered-derivative symbol divided by n, or with
+// raw=true the reference's own (unnormalised, possibly non-Hermitian) symbol.
 // which: 0 = x velocity derivative, 1 = x pressure derivative,
 //        2 = z velocity derivative, 3 = z pressure derivative.
-void shift_symbols(int n, double d, int which, std::vector<std::complex<double>>& H);
+void shift_symbols(int n, double d, int which, std::vector<std::complex<double>>& H, bool raw = false);
 
 struct HostPlan {
     int n = 0, m = 0, blue = 0;

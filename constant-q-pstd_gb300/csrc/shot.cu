@@ -215,6 +215,12 @@ static int setup_visco(qpstd_shot* s, const qpstd_shot_desc* d) {
         h[6 * N + i] = (float)(dt * tao);
     }
     CK(cudaMemcpy(f, h.data(), sizeof(float) * 7 * N, cudaMemcpyHostToDevice));
+    return QPSTD_OK;
+}
+
+// Squared wavenumbers kkx^2, kkz^2 (the 2-D symbols are built from them on the fly).
+static int setup_ksq(qpstd_shot* s, const qpstd_shot_desc* d) {
+    int rc = QPSTD_OK;
     std::vector<float> k2(d->nxx + d->nzz);
     for (int i = 0; i < d->nxx; i++) {
         const double k = wavenumber(i, d->nxx, d->dx);
@@ -229,6 +235,29 @@ static int setup_visco(qpstd_shot* s, const qpstd_shot_desc* d) {
     CK(cudaMemcpy(kk, k2.data(), sizeof(float) * k2.size(), cudaMemcpyHostToDevice));
     s->kxsq = kk;
     s->kzsq = kk + d->nxx;
+    return QPSTD_OK;
+}
+
+// Plain form: cuFFT plan, scratch, and the reference's own shift symbols.
+static int setup_plain(qpstd_shot* s, const qpstd_shot_desc* d) {
+    std::string err;
+    if (plain_setup(s, err)) return fail(QPSTD_ECUDA, err);
+    const int lens[4] = {d->nxx, d->nxx, d->nzz, d->nzz};
+    const double sp[4] = {d->dx, d->dx, d->dz, d->dz};
+    const size_t nc = 2 * (size_t)d->nxx + 2 * d->nzz;
+    std::vector<float2> hc(nc);
+    float2* cbase = nullptr;
+    CK(cudaMalloc(&cbase, sizeof(float2) * nc));
+    s->allocs.push_back(cbase);
+    const float2** dst[4] = {&s->plain.HxM, &s->plain.HxP, &s->plain.HzM, &s->plain.HzP};
+    size_t q = 0;
+    std::vector<std::complex<double>> H;
+    for (int w = 0; w < 4; w++) {
+        shift_symbols(lens[w], sp[w], w, H, true);
+        *dst[w] = cbase + q;
+        for (auto& c : H) hc[q++] = make_float2((float)c.real(), (float)c.imag());
+    }
+    CK(cudaMemcpy(cbase, hc.data(), sizeof(float2) * nc, cudaMemcpyHostToDevice));
     return QPSTD_OK;
 }
 
@@ -251,7 +280,6 @@ extern "C" int qpstd_shot_create(const qpstd_shot_desc* d, qpstd_shot** out) {
         qpstd_shot_destroy(s);
         return code;
     };
-    if (d->method == QPSTD_PLAIN) return bail(fail(QPSTD_ENOTSUP, "plain method not built yet"));
     static int smem_ok = -1;
     if (smem_ok != 0) smem_ok = (ac_set_smem_limits() || vz_set_smem_limits()) ? -1 : 0;
     s->nzh = nzz / 2 + 1;
@@ -346,6 +374,8 @@ extern "C" int qpstd_shot_create(const qpstd_shot_desc* d, qpstd_shot** out) {
             return bail(fail(QPSTD_ENOTSUP, "line too long for one CTA"));
     }
     if (s->visco && (rc = setup_visco(s, d))) return bail(rc);
+    if ((rc = setup_ksq(s, d))) return bail(rc);
+    if (d->method == QPSTD_PLAIN && (rc = setup_plain(s, d))) return bail(rc);
     if ((rc = build_receivers(s, d))) return bail(rc);
     s->gather = dalloc(s, (size_t)d->nt * std::max(d->nr, 1), &rc);
     if (!s->gather) return bail(rc);
@@ -371,6 +401,7 @@ extern "C" int qpstd_shot_destroy(qpstd_shot* s) {
         cudaEventDestroy(t.b);
     }
     for (cudaEvent_t e : s->evpool) cudaEventDestroy(e);
+    plain_release(s);
     for (void* p : s->allocs) cudaFree(p);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
@@ -408,12 +439,12 @@ struct ProfScope {
     qpstd_shot* s;
     int kind;
     cudaEvent_t a = nullptr;
-    ProfScope(qpstd_shot* s_, int k) : s(s_), kind(k) {
+    ProfScope(qpstd_shot* s_, int k, int count = 1) : s(s_), kind(k) {
         if (s->prof) {
             a = pool_event(s);
             cudaEventRecord(a, s->stream);
         }
-        s->launches++;
+        s->launches += count;
     }
     ~ProfScope() {
         if (s->prof) {
@@ -493,8 +524,17 @@ static AcXArgs xargs(qpstd_shot* s, Wave& w, int do_p, int do_v, int do_dx) {
 // end() applies the last step's pending z-velocity update.  Between end() and
 // the next begin() the eight state fields are exactly the reference's state.
 static void src_begin(qpstd_shot* s) {
+    if (s->d.method == QPSTD_PLAIN) return;  // the plain form keeps no state between steps
     ProfScope ps(s, QPSTD_K_XPASS);
     launch_ac_xpass(xargs(s, s->src, 0, 0, 1), s->stream);
+}
+
+// One plain-form step (all of its cuFFT calls and kernels timed as one unit).
+static void plain_one(qpstd_shot* s, Wave& w, float src, int t_filter, float eta, float* gather_row,
+                      const float* obs_row, bool ssg_on, bool image) {
+    ProfScope ps(s, QPSTD_K_PLAIN, 0);
+    const int rc = plain_step(s, w, src, t_filter, eta, gather_row, obs_row, ssg_on, image, &s->launches);
+    if (rc && !s->plain_err) s->plain_err = rc;
 }
 
 // One constant-Q step of wavefield w (seven launches, see vz_kernels.cu).
@@ -601,6 +641,10 @@ static float src_amp(qpstd_shot* s, int t) {
 // illumination (first sweep of RTM, addsa_kernel restart==0).
 static void src_step(qpstd_shot* s, int t, bool first, bool last, float* gather_row, bool ssg_on) {
     Wave& w = s->src;
+    if (s->d.method == QPSTD_PLAIN) {
+        plain_one(s, w, src_amp(s, t), t, s->d.etas, gather_row, nullptr, ssg_on, false);
+        return;
+    }
     if (s->visco) {
         vz_step(s, w, src_amp(s, t), t, s->d.etas, last, gather_row, nullptr, ssg_on, false);
         return;
@@ -625,6 +669,7 @@ static void src_step(qpstd_shot* s, int t, bool first, bool last, float* gather_
 }
 
 static void src_end(qpstd_shot* s) {
+    if (s->d.method == QPSTD_PLAIN) return;
     if (s->visco) {
         vz_finish(s, s->src);
         return;
@@ -641,6 +686,7 @@ static int advance_src(qpstd_shot* s, int t0, int n, float* gather, bool ssg_on)
     for (int t = t0; t < t0 + n; t++)
         src_step(s, t, t == t0, t == t0 + n - 1, gather ? gather + (size_t)(t - t0) * s->d.nr : nullptr, ssg_on);
     src_end(s);
+    if (s->plain_err) return fail(QPSTD_ECUDA, "plain step failed (cuFFT or launch)");
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
     return QPSTD_OK;
@@ -678,6 +724,11 @@ extern "C" int qpstd_shot_pipeline_end(qpstd_shot* s) {
 static int receiver_step(qpstd_shot* s, int row, bool first) {
     Wave& w = s->rcv;
     cudaStream_t st = s->stream;
+    if (s->d.method == QPSTD_PLAIN) {
+        plain_one(s, w, 0.f, row, s->d.etar, nullptr, s->obs + (size_t)row * s->d.nr, false, true);
+        if (s->plain_err) return fail(QPSTD_ECUDA, "plain step failed (cuFFT or launch)");
+        return QPSTD_OK;
+    }
     if (s->visco) {
         // addsa_b_kernel + multt_kernel(etar, nt = row), sgpstd-qrtm/acsglw.cu:745-776, 907-940
         vz_step(s, w, 0.f, row, s->d.etar, false, nullptr, s->obs + (size_t)row * s->d.nr, false, true);

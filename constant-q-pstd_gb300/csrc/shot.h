@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "../../include/qpstd.h"
+#include "plain.h"
 #include "qpstd_internal.h"
 
 namespace qp {
@@ -59,6 +60,9 @@ struct qpstd_shot {
     float *kxsq = nullptr, *kzsq = nullptr;   // unnormalised squared wavenumbers
     int* rec_off_z = nullptr;                  // receivers keyed by z-pass tile
     qp::RecEntry* rec_z = nullptr;
+    // plain (cuFFT) form
+    qp::PlainState plain;
+    int plain_err = 0;
     std::vector<float> rik;
     float* gather = nullptr;
     float* store = nullptr;

@@ -136,18 +136,23 @@ __global__ void __launch_bounds__(768, 1) vz_xspec_kernel(VxsArgs a) {
         for (int ix = threadIdx.x; ix < nxx; ix += blockDim.x) X[threadIdx.y * ld + ix] = line[ix];
         __syncthreads();
     }
-    for (int j = 0; j < nout; j++) {
+    // outputs written out in sequence (a loop here costs register spills)
+    auto output = [&](int j, float2* out) {
         const float2* src = (nout == 3) ? X + threadIdx.y * ld : line;
         for (int ix = threadIdx.x; ix < nxx; ix += blockDim.x)
             line[ix] = cscale(src[ix], spec_symbol(a, j, a.kx2[ix] + kzsq) * a.norm);
         __syncthreads();
         dft_n<+1>(smem, ld, fc, L);
-        float2* out = (j == 0) ? a.out0 : ((j == 1) ? a.out1 : a.out2);
         for (int g = t0; g < tot; g += nthr) {
             const int c = g & (L - 1), ix = g >> lg;
             if (kz0 + c < nzh) out[(size_t)ix * nzh + kz0 + c] = smem[c * ld + ix];
         }
         __syncthreads();
+    };
+    output(0, a.out0);
+    if (nout == 3) {
+        output(1, a.out1);
+        output(2, a.out2);
     }
 }
 
@@ -156,22 +161,23 @@ __global__ void __launch_bounds__(768, 1) vz_passB_kernel(VzArgsB a) {
     ZPASS_SETUP
     const int nzh = a.nzh;
     float2* acc = smem + (size_t)(L + threadIdx.y) * ld;  // running total of this line pair
-    for (int j = 0; j < 3; j++) {
-        const float2* spec = (j == 0) ? a.Y2 : ((j == 1) ? a.Y3 : a.Y4);
-        const float* cf = (j == 0) ? a.y2 : ((j == 1) ? a.y3c : a.y4c);
-        const float sg = (j == 0) ? 1.f : -1.f;
+    // three terms, written out in sequence (a loop here costs register spills)
+    auto term = [&](const float2* spec, const float* cf, float sg, bool first) {
         zrepack(spec, line, nzz, nzh, has0, has1, xa);
         __syncthreads();
         dft_n<+1>(smem, ld, fc, L);
         for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
             const float2 y = line[k];
-            float2 t = (j == 0) ? make_float2(0.f, 0.f) : acc[k];
+            float2 t = first ? make_float2(0.f, 0.f) : acc[k];
             if (has0) t.x += sg * cf[r0 + k] * y.x;
             if (has1) t.y += sg * cf[r1 + k] * y.y;
             acc[k] = t;
         }
         __syncthreads();
-    }
+    };
+    term(a.Y2, a.y2, 1.f, true);
+    term(a.Y3, a.y3c, -1.f, false);
+    term(a.Y4, a.y4c, -1.f, false);
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 t = acc[k];
         float2 v = make_float2(0.f, 0.f);

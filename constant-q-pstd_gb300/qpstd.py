@@ -75,7 +75,7 @@ EXPORTS = {
     "qpstd_shot_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "qpstd_shot_profile_read": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
 }
-KIND_NAMES = ["xpass", "zpass", "xspec", "other"]
+KIND_NAMES = ["xpass", "zpass", "xspec", "other", "plain"]
 
 
 def lib():

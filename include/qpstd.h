@@ -129,7 +129,8 @@ void *qpstd_shot_stream(qpstd_shot *s);
 #define QPSTD_K_ZPASS 1   /* z-line pass (real fields) */
 #define QPSTD_K_XSPEC 2   /* x-line pass over z-spectra (2-D isotropic operators) */
 #define QPSTD_K_OTHER 3   /* small helpers (checkpoint-0 source sample, filters) */
-#define QPSTD_NKINDS 4
+#define QPSTD_K_PLAIN 4   /* one whole plain-form step (cuFFT calls + elementwise kernels) */
+#define QPSTD_NKINDS 5
 int qpstd_shot_set_profiling(qpstd_shot *s, int on);
 int qpstd_shot_profile_read(qpstd_shot *s, int nkinds, double *ms, long long *count);
 
