@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(768, 1) ac_zpass_kernel(AcZArgs a) {
     if (a.do_v) {
         zload_pair(a.p, line, nzz, has0, has1, r0, r1);
         __syncthreads();
-        roundtrip_c(smem, ld, fc, L, a.HzP);
+        roundtrip_conv(smem, ld, fc, L, a.HzP);
         for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
             const float2 d = line[k];
             const float hb = a.h_bz[k], ha = a.h_az[k];
@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(768, 1) ac_zpass_kernel(AcZArgs a) {
     }
     if (!a.do_div) return;
     __syncthreads();
-    roundtrip_c(smem, ld, fc, L, a.HzM);
+    roundtrip_conv(smem, ld, fc, L, a.HzM);
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 d = line[k];
         const float ib = a.i_bz[k], ia = a.i_az[k];
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(768, 1) ac_zpass_kernel(AcZArgs a) {
         line[k] = dv;
     }
     __syncthreads();
-    roundtrip_r(smem, ld, fc, L, a.kz2);
+    roundtrip_conv(smem, ld, fc, L, a.kz2);
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 d = line[k];
         if (has0) a.Lz[r0 + k] = d.x;
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
     if (a.do_p) {
         xload(a.div, sf, T, ld);
         __syncthreads();
-        roundtrip_r(smem, ld, fc, L, a.kx2);
+        roundtrip_conv(smem, ld, fc, L, a.kx2);
         for (int g = T.t0; g < T.tot; g += T.nthr) {
             int c, ix;
             T.split(g, c, ix);
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
     if (a.do_v) {
         if (!have) xload(a.p, sf, T, ld);
         __syncthreads();
-        roundtrip_c(smem, ld, fc, L, a.HxP);
+        roundtrip_conv(smem, ld, fc, L, a.HxP);
         for (int g = T.t0; g < T.tot; g += T.nthr) {
             int c, ix;
             T.split(g, c, ix);
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
     if (a.do_dx) {
         if (!have) xload(a.vx, sf, T, ld);
         __syncthreads();
-        roundtrip_c(smem, ld, fc, L, a.HxM);
+        roundtrip_conv(smem, ld, fc, L, a.HxM);
         for (int g = T.t0; g < T.tot; g += T.nthr) {
             int c, ix;
             T.split(g, c, ix);

@@ -294,6 +294,27 @@ template <int S> __device__ __forceinline__ void dft_n(float2* buf, int ld, cons
     __syncthreads();
 }
 
+// Separable operator as a zero-padded circular convolution on a length-m
+// plan: y[0,n) = IFFT_m(Hm .* FFT_m(x zero-padded to m)), Hm from conv_table
+// (m = n when n itself is smooth).  Caller has synchronised after filling
+// entries [0,n); ends with a barrier.
+__device__ __forceinline__ void roundtrip_conv(float2* buf, int ld, const FFTCtx& pl, int L,
+                                               const float2* __restrict__ Hm) {
+    const int l = threadIdx.y;
+    float2* line = buf + l * ld;
+    const bool act = l < L;
+    if (pl.m > pl.n) {
+        if (act)
+            for (int k = pl.n + threadIdx.x; k < pl.m; k += blockDim.x) line[k] = make_float2(0.f, 0.f);
+        __syncthreads();
+    }
+    fft_m<-1>(buf, ld, pl, L);
+    if (act)
+        for (int k = threadIdx.x; k < pl.m; k += blockDim.x) line[k] = cmul(line[k], __ldg(&Hm[k]));
+    __syncthreads();
+    fft_m<+1>(buf, ld, pl, L);
+}
+
 // y = IDFT(H .* DFT(x)) with a complex symbol (length n, 1/n folded in).
 __device__ __forceinline__ void roundtrip_c(float2* buf, int ld, const FFTCtx& pl, int L,
                                             const float2* __restrict__ H) {

@@ -253,4 +253,63 @@ int build_plan_host(int n, HostPlan& hp) {
     return 0;
 }
 
+// A separable spectral operator y = IDFT_n(H . DFT_n(x)) is the circular
+// convolution of x with h = IDFT_n(H).  Any length m >= 2n-1 computes it with
+// one zero-padded forward and one inverse length-m FFT (every lag i-j in
+// (-n, n) lands on a distinct slot of the length-m wrap), so a window length
+// with a large prime factor costs two smooth FFTs instead of Bluestein's four.
+int build_conv_plan_host(int n, HostPlan& hp) {
+    hp = HostPlan();
+    hp.n = n;
+    if (n == 1 || factor_direct(n, hp.rad)) {
+        hp.m = (n == 1) ? 1 : n;
+        if (n == 1) hp.rad.clear();
+    } else {
+        double best = 1e300;
+        for (int m = 2 * n - 1; m <= (int)(2.3 * n) + 8; m++) {
+            if (!smooth7(m)) continue;
+            std::vector<int> r;
+            if (!factor_direct(m, r)) continue;
+            const double cost = (double)m * r.size();
+            if (cost < best) {
+                best = cost;
+                hp.m = m;
+                hp.rad = r;
+            }
+        }
+        if (best == 1e300) return -1;
+    }
+    hp.w.resize(hp.m);
+    for (int k = 0; k < hp.m; k++) {
+        const double a = -2.0 * M_PI * (double)k / (double)hp.m;
+        hp.w[k] = std::complex<double>(std::cos(a), std::sin(a));
+    }
+    return 0;
+}
+
+// Spectrum (length m, 1/m folded in) of the zero-padded, wrapped kernel of the
+// operator whose length-n symbol is Hn (1/n already folded in).
+void conv_table(const HostPlan& hp, const std::vector<std::complex<double>>& Hn,
+                std::vector<std::complex<double>>& out) {
+    const int n = hp.n, m = hp.m;
+    if (m == n) {
+        out = Hn;
+        return;
+    }
+    // h[d] = sum_k Hn[k] e^{+2 pi i k d / n}, exact phases from (k d) mod n
+    std::vector<std::complex<double>> h(n), e(n);
+    for (int q = 0; q < n; q++) e[q] = std::complex<double>(std::cos(2.0 * M_PI * q / n), std::sin(2.0 * M_PI * q / n));
+    for (int d = 0; d < n; d++) {
+        std::complex<double> acc = 0.0;
+        for (int k = 0; k < n; k++) acc += Hn[k] * e[(int)(((long long)k * d) % n)];
+        h[d] = acc;
+    }
+    std::vector<std::complex<double>> hm(m, 0.0);
+    for (int d = 0; d < n; d++) hm[d] = h[d];               // lags 0 .. n-1
+    for (int d = 1; d < n; d++) hm[m - d] = h[n - d];       // lags -(n-1) .. -1
+    host_fft(hm, hp.rad, -1);
+    out.resize(m);
+    for (int k = 0; k < m; k++) out[k] = hm[k] / (double)m;
+}
+
 }  // namespace qp

@@ -25,5 +25,11 @@ struct HostPlan {
     std::vector<std::complex<double>> w, chirp, bhat;
 };
 int build_plan_host(int n, HostPlan& hp);
+// Length-m FFT plan for separable operators applied as zero-padded circular
+// convolutions (m = n when n factors into radices <= 16, else smooth m >= 2n-1).
+int build_conv_plan_host(int n, HostPlan& hp);
+// Length-m multiplier of the convolution form of the symbol Hn (1/n folded in).
+void conv_table(const HostPlan& hp, const std::vector<std::complex<double>>& Hn,
+                std::vector<std::complex<double>>& out);
 
 }  // namespace qp

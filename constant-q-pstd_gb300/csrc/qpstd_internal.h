@@ -43,11 +43,13 @@ struct RecEntry {
 //   do_v  : Pz = dz+ p; psi_pz; vz += dt bbz (Pz + psi_pz)
 //   do_div: Dz = dz- vz; psi_vz; div = Dx + Dz + psi_vz; Lz = F^-1[kz^2 F div]
 // ---------------------------------------------------------------------------
+// The operators are applied as zero-padded circular convolutions on the
+// length-m convolution plan pl; HzP, HzM, kz2 are their length-m multipliers.
 struct AcZArgs {
     int nxx, nzz, L;
     FFTPlanDev pl;
     const float2 *HzP, *HzM;
-    const float* kz2;
+    const float2* kz2;
     const float *h_az, *h_bz, *i_az, *i_bz;
     const float* bbz;
     float *p, *vz, *psi_pz, *psi_vz;
@@ -67,9 +69,9 @@ struct AcZArgs {
 // ---------------------------------------------------------------------------
 struct AcXArgs {
     int nxx, nzz, L, pml;
-    FFTPlanDev pl;
-    const float2 *HxP, *HxM;
-    const float* kx2;
+    FFTPlanDev pl;                // convolution plan along x
+    const float2 *HxP, *HxM;      // length-m convolution multipliers
+    const float2* kx2;
     const float *h_ax, *h_bx, *i_ax, *i_bx;
     const float *bbx, *c1, *c2;
     float *p, *vx, *psi_px, *psi_vx, *Dx;
@@ -100,8 +102,9 @@ struct AcXArgs {
 // div -> half spectrum G.
 struct VzArgsA {
     int nxx, nzz, nzh, L;
-    FFTPlanDev pl;
-    const float2* HzM;
+    FFTPlanDev pl;            // exact length-nzz DFT plan (spectra)
+    FFTPlanDev plc;           // convolution plan for the z derivative
+    const float2* HzM;        // convolution multiplier on plc
     const float *i_az, *i_bz;
     const float2* aux_spec;   // spectrum of the previous step's aux (null: aux already real)
     float* aux;

@@ -261,6 +261,51 @@ static int setup_plain(qpstd_shot* s, const qpstd_shot_desc* d) {
     return QPSTD_OK;
 }
 
+// Convolution plans along x and z and the length-m multipliers of the six
+// separable operators (two staggered derivatives and the k^2 term per axis).
+static int setup_conv(qpstd_shot* s, const qpstd_shot_desc* d) {
+    HostPlan cx, cz;
+    if (build_conv_plan_host(d->nxx, cx) || build_conv_plan_host(d->nzz, cz))
+        return fail(QPSTD_ENOTSUP, "no convolution plan for this length");
+    int rc;
+    if ((rc = upload_plan(s, cx, s->pxc))) return rc;
+    if ((rc = upload_plan(s, cz, s->pzc))) return rc;
+    const size_t nc = 3 * (size_t)cx.m + 3 * (size_t)cz.m;
+    std::vector<float2> hc(nc);
+    float2* base = nullptr;
+    CK(cudaMalloc(&base, sizeof(float2) * nc));
+    s->allocs.push_back(base);
+    size_t q = 0;
+    std::vector<std::complex<double>> H, T;
+    auto put = [&](const HostPlan& hp, const std::vector<std::complex<double>>& sym, const float2** dst) {
+        conv_table(hp, sym, T);
+        *dst = base + q;
+        for (auto& c : T) hc[q++] = make_float2((float)c.real(), (float)c.imag());
+    };
+    shift_symbols(d->nxx, d->dx, 0, H);
+    put(cx, H, &s->cHxM);
+    shift_symbols(d->nxx, d->dx, 1, H);
+    put(cx, H, &s->cHxP);
+    H.assign(d->nxx, 0.0);
+    for (int i = 0; i < d->nxx; i++) {
+        const double k = wavenumber(i, d->nxx, d->dx);
+        H[i] = k * k / d->nxx;
+    }
+    put(cx, H, &s->cKx2);
+    shift_symbols(d->nzz, d->dz, 2, H);
+    put(cz, H, &s->cHzM);
+    shift_symbols(d->nzz, d->dz, 3, H);
+    put(cz, H, &s->cHzP);
+    H.assign(d->nzz, 0.0);
+    for (int j = 0; j < d->nzz; j++) {
+        const double k = wavenumber(j, d->nzz, d->dz);
+        H[j] = k * k / d->nzz;
+    }
+    put(cz, H, &s->cKz2);
+    CK(cudaMemcpy(base, hc.data(), sizeof(float2) * nc, cudaMemcpyHostToDevice));
+    return QPSTD_OK;
+}
+
 extern "C" int qpstd_shot_create(const qpstd_shot_desc* d, qpstd_shot** out) {
     if (!out) return fail(QPSTD_EINVAL, "null output handle");
     *out = nullptr;
@@ -363,15 +408,17 @@ extern "C" int qpstd_shot_create(const qpstd_shot_desc* d, qpstd_shot** out) {
         if (build_plan_host(nxx, hx) || build_plan_host(nzz, hz)) return bail(fail(QPSTD_ENOTSUP, "no FFT plan for this length"));
         if ((rc = upload_plan(s, hx, s->px))) return bail(rc);
         if ((rc = upload_plan(s, hz, s->pz))) return bail(rc);
+        if ((rc = setup_conv(s, d))) return bail(rc);
         const int pairs_z = (nxx + 1) / 2, pairs_x = (nzz + 1) / 2;
-        s->Lx = choose_L(pairs_x, s->px.m, s->px.tx, 1, true);
-        s->Lzp = choose_L(pairs_z, s->pz.m, s->pz.tx, 1, false);
-        // constant-Q: z pass B and the 3-output x-spectral pass hold two line buffers
-        s->Lzv = choose_L(pairs_z, s->pz.m, s->pz.tx, 2, false);
+        s->Lx = choose_L(pairs_x, s->pxc.m, s->pxc.tx, 1, true);
+        s->Lzp = choose_L(pairs_z, s->pzc.m, s->pzc.tx, 1, false);
+        // constant-Q: z pass B and the 3-output x-spectral pass hold two line buffers;
+        // z pass A uses both the exact and the convolution plan
+        s->Lzv = choose_L(pairs_z, std::max(s->pz.m, s->pzc.m), std::max(s->pz.tx, s->pzc.tx), 2, false);
         s->Lxs = choose_L(s->nzh, s->px.m, s->px.tx, 1, true);
         s->Lxs3 = choose_L(s->nzh, s->px.m, s->px.tx, 2, true);
-        if (16.0 * s->px.m > 200 * 1024 || 16.0 * s->pz.m > 200 * 1024)
-            return bail(fail(QPSTD_ENOTSUP, "line too long for one CTA"));
+        const int mmax = std::max(std::max(s->px.m, s->pz.m), std::max(s->pxc.m, s->pzc.m));
+        if (16.0 * mmax > 200 * 1024) return bail(fail(QPSTD_ENOTSUP, "line too long for one CTA"));
     }
     if (s->visco && (rc = setup_visco(s, d))) return bail(rc);
     if ((rc = setup_ksq(s, d))) return bail(rc);
@@ -462,10 +509,10 @@ static AcZArgs zargs(qpstd_shot* s, Wave& w, int do_v, int do_div) {
     a.nxx = s->d.nxx;
     a.nzz = s->d.nzz;
     a.L = s->Lzp;
-    a.pl = s->pz;
-    a.HzP = s->HzP;
-    a.HzM = s->HzM;
-    a.kz2 = s->kz2;
+    a.pl = s->pzc;
+    a.HzP = s->cHzP;
+    a.HzM = s->cHzM;
+    a.kz2 = s->cKz2;
     a.h_az = s->h_az;
     a.h_bz = s->h_bz;
     a.i_az = s->i_az;
@@ -491,10 +538,10 @@ static AcXArgs xargs(qpstd_shot* s, Wave& w, int do_p, int do_v, int do_dx) {
     a.nzz = s->d.nzz;
     a.L = s->Lx;
     a.pml = s->d.pml;
-    a.pl = s->px;
-    a.HxP = s->HxP;
-    a.HxM = s->HxM;
-    a.kx2 = s->kx2;
+    a.pl = s->pxc;
+    a.HxP = s->cHxP;
+    a.HxM = s->cHxM;
+    a.kx2 = s->cKx2;
     a.h_ax = s->h_ax;
     a.h_bx = s->h_bx;
     a.i_ax = s->i_ax;
@@ -550,8 +597,8 @@ static void vz_step(qpstd_shot* s, Wave& w, float src, int t_filter, float eta, 
     const float norm = (float)(1.0 / ((double)nxx * nzz));
     {
         VzArgsA a{};
-        a.nxx = nxx; a.nzz = nzz; a.nzh = nzh; a.L = s->Lzv; a.pl = s->pz;
-        a.HzM = s->HzM; a.i_az = s->i_az; a.i_bz = s->i_bz;
+        a.nxx = nxx; a.nzz = nzz; a.nzh = nzh; a.L = s->Lzv; a.pl = s->pz; a.plc = s->pzc;
+        a.HzM = s->cHzM; a.i_az = s->i_az; a.i_bz = s->i_bz;
         a.aux_spec = w.aux_pending ? w.aux_spec : nullptr;
         a.aux = w.aux(N); a.vz = w.vz(N); a.psi_vz = w.fivzz(N); a.Dx = w.Dx(N);
         a.div = s->div; a.G = s->spec[0];

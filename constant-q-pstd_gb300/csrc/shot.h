@@ -47,7 +47,10 @@ struct qpstd_shot {
     const float *h_ax = nullptr, *h_bx = nullptr, *h_az = nullptr, *h_bz = nullptr;
     const float *kx2 = nullptr, *kz2 = nullptr;
     const float2 *HxM = nullptr, *HxP = nullptr, *HzM = nullptr, *HzP = nullptr;
-    qp::FFTPlanDev px{}, pz{};
+    qp::FFTPlanDev px{}, pz{};      // exact DFT plans (spectra of the constant-Q operators)
+    qp::FFTPlanDev pxc{}, pzc{};    // convolution plans (separable operators)
+    const float2 *cHxM = nullptr, *cHxP = nullptr, *cKx2 = nullptr;  // convolution multipliers
+    const float2 *cHzM = nullptr, *cHzP = nullptr, *cKz2 = nullptr;
     int Lx = 1, Lzp = 1, ntile_x = 0;
     int* rec_off = nullptr;
     qp::RecEntry* rec = nullptr;

@@ -57,7 +57,16 @@ __device__ __forceinline__ void zunpack(const float2* line, float2* __restrict__
 
 // ---- z pass A ---------------------------------------------------------------
 __global__ void __launch_bounds__(768, 1) vz_passA_kernel(VzArgsA a) {
-    ZPASS_SETUP
+    extern __shared__ float2 smem[];
+    __shared__ FFTPass s_pass[QP_MAXST];
+    __shared__ FFTPass s_pass_c[QP_MAXST];
+    const FFTCtx fc = make_ctx(a.pl, s_pass);
+    const FFTCtx fcc = make_ctx(a.plc, s_pass_c);
+    const int L = a.L, ld = max(a.pl.m, a.plc.m), nzz = a.nzz, nxx = a.nxx;
+    float2* line = smem + threadIdx.y * ld;
+    const int xa = blockIdx.x * 2 * L + 2 * threadIdx.y;
+    const bool has0 = xa < nxx, has1 = xa + 1 < nxx;
+    const size_t r0 = (size_t)xa * nzz, r1 = r0 + nzz;
     const int nzh = a.nzh;
     if (a.aux_spec) {
         zrepack(a.aux_spec, line, nzz, nzh, has0, has1, xa);
@@ -72,7 +81,7 @@ __global__ void __launch_bounds__(768, 1) vz_passA_kernel(VzArgsA a) {
     }
     zload_pair(a.vz, line, nzz, has0, has1, r0, r1);
     __syncthreads();
-    roundtrip_c(smem, ld, fc, L, a.HzM);
+    roundtrip_conv(smem, ld, fcc, L, a.HzM);
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 d = line[k];
         const float ib = a.i_bz[k], ia = a.i_az[k];
@@ -294,7 +303,7 @@ static size_t lsm(int L, int m, int nbuf) { return sizeof(float2) * (size_t)nbuf
 static int zgrid(int nxx, int L) { return (nxx + 2 * L - 1) / (2 * L); }
 
 void launch_vz_passA(const VzArgsA& a, cudaStream_t s) {
-    vz_passA_kernel<<<zgrid(a.nxx, a.L), dim3(a.pl.tx, a.L), lsm(a.L, a.pl.m, 1), s>>>(a);
+    vz_passA_kernel<<<zgrid(a.nxx, a.L), dim3(max(a.pl.tx, a.plc.tx), a.L), lsm(a.L, max(a.pl.m, a.plc.m), 1), s>>>(a);
 }
 void launch_vz_xspec(const VxsArgs& a, cudaStream_t s) {
     vz_xspec_kernel<<<(a.nzh + a.L - 1) / a.L, dim3(a.pl.tx, a.L), lsm(a.L, a.pl.m, a.mode == 0 ? 2 : 1), s>>>(a);
