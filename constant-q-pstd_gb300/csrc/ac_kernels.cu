@@ -9,16 +9,20 @@
 //   x pass : kx^2 part of L -> p update (+ source, receivers, illumination,
 //            imaging, Dirichlet injection) ; dx+ p -> CPML -> vx update ;
 //            dx- vx -> CPML (x part of the next step's divergence)
-// Each derivative is a forward line DFT, a multiply by the Hermitian part of
-// the reference's shift symbol, and an inverse line DFT, all in shared memory.
-// Blocks are (TX, L): TX threads per complex line, L lines; a z-pass CTA owns
-// 2L consecutive x indices, an x-pass CTA owns 2L consecutive z indices.
+// Each operator is a zero-padded circular convolution done with two
+// shared-memory line FFTs (fft_reg.cuh); the multiplier is the Hermitian part
+// of the reference's symbol.  Blocks are (TX, L): TX threads per complex line,
+// L lines; a z-pass CTA owns 2L consecutive x indices, an x-pass CTA owns 2L
+// consecutive z indices.  When a.stage is set, the inputs of the epilogues
+// are copied to shared memory asynchronously at kernel start (cp.async), so
+// their latency overlaps the FFTs.
 #include "fft_reg.cuh"
 #include "pass_common.cuh"
 
 namespace qp {
 
 // ---- z pass ----------------------------------------------------------------
+// staged fields (each L*2*nzz floats): 0 vz, 1 psi_pz, 2 bbz, 3 psi_vz, 4 Dx
 __global__ void __launch_bounds__(768, 1) ac_zpass_kernel(AcZArgs a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
@@ -28,25 +32,55 @@ __global__ void __launch_bounds__(768, 1) ac_zpass_kernel(AcZArgs a) {
     const int xa = blockIdx.x * 2 * L + 2 * threadIdx.y;  // first x of this thread's line pair
     const bool has0 = xa < nxx, has1 = xa + 1 < nxx;
     const size_t r0 = (size_t)xa * nzz, r1 = r0 + nzz;
+    const size_t fstride = (size_t)L * 2 * nzz;
+    float* stg = reinterpret_cast<float*>(smem + (size_t)L * ld) + (size_t)threadIdx.y * 2 * nzz;
+    auto S = [&](int f, int row, int k) -> float& { return stg[f * fstride + row * nzz + k]; };
+    const float* vz_in = a.vz;
+    const float* ppz_in = a.psi_pz;
+    const float* bbz_in = a.bbz;
+    const float* pvz_in = a.psi_vz;
+    const float* dx_in = a.Dx;
+    if (a.stage) {
+        for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+            for (int h = 0; h < 2; h++) {
+                if (!(h ? has1 : has0)) continue;
+                const size_t i = (h ? r1 : r0) + k;
+                if (a.do_v) {
+                    cp_async4(&S(0, h, k), a.vz + i);
+                    cp_async4(&S(1, h, k), a.psi_pz + i);
+                    cp_async4(&S(2, h, k), a.bbz + i);
+                }
+                if (a.do_div) {
+                    cp_async4(&S(3, h, k), a.psi_vz + i);
+                    cp_async4(&S(4, h, k), a.Dx + i);
+                }
+            }
+        }
+        cp_async_commit();
+    }
+    auto rd = [&](int f, const float* g, int h, int k) -> float {
+        return a.stage ? S(f, h, k) : g[(h ? r1 : r0) + k];
+    };
 
     if (a.do_v) {
         zload_pair(a.p, line, nzz, has0, has1, r0, r1);
         __syncthreads();
         roundtrip_conv(smem, ld, fc, L, a.HzP);
+        if (a.stage) cp_async_wait_all();
         for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
             const float2 d = line[k];
             const float hb = a.h_bz[k], ha = a.h_az[k];
             float2 nv = make_float2(0.f, 0.f);
             if (has0) {
-                const float ps = hb * a.psi_pz[r0 + k] + ha * d.x;
+                const float ps = hb * rd(1, ppz_in, 0, k) + ha * d.x;
                 a.psi_pz[r0 + k] = ps;
-                nv.x = a.vz[r0 + k] + a.dt * a.bbz[r0 + k] * (d.x + ps);
+                nv.x = rd(0, vz_in, 0, k) + a.dt * rd(2, bbz_in, 0, k) * (d.x + ps);
                 a.vz[r0 + k] = nv.x;
             }
             if (has1) {
-                const float ps = hb * a.psi_pz[r1 + k] + ha * d.y;
+                const float ps = hb * rd(1, ppz_in, 1, k) + ha * d.y;
                 a.psi_pz[r1 + k] = ps;
-                nv.y = a.vz[r1 + k] + a.dt * a.bbz[r1 + k] * (d.y + ps);
+                nv.y = rd(0, vz_in, 1, k) + a.dt * rd(2, bbz_in, 1, k) * (d.y + ps);
                 a.vz[r1 + k] = nv.y;
             }
             line[k] = nv;
@@ -57,20 +91,21 @@ __global__ void __launch_bounds__(768, 1) ac_zpass_kernel(AcZArgs a) {
     if (!a.do_div) return;
     __syncthreads();
     roundtrip_conv(smem, ld, fc, L, a.HzM);
+    if (a.stage) cp_async_wait_all();
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 d = line[k];
         const float ib = a.i_bz[k], ia = a.i_az[k];
         float2 dv = make_float2(0.f, 0.f);
         if (has0) {
-            const float ps = ib * a.psi_vz[r0 + k] + ia * d.x;
+            const float ps = ib * rd(3, pvz_in, 0, k) + ia * d.x;
             a.psi_vz[r0 + k] = ps;
-            dv.x = a.Dx[r0 + k] + (d.x + ps);
+            dv.x = rd(4, dx_in, 0, k) + (d.x + ps);
             a.div[r0 + k] = dv.x;
         }
         if (has1) {
-            const float ps = ib * a.psi_vz[r1 + k] + ia * d.y;
+            const float ps = ib * rd(3, pvz_in, 1, k) + ia * d.y;
             a.psi_vz[r1 + k] = ps;
-            dv.y = a.Dx[r1 + k] + (d.y + ps);
+            dv.y = rd(4, dx_in, 1, k) + (d.y + ps);
             a.div[r1 + k] = dv.y;
         }
         line[k] = dv;
@@ -85,6 +120,8 @@ __global__ void __launch_bounds__(768, 1) ac_zpass_kernel(AcZArgs a) {
 }
 
 // ---- x pass ----------------------------------------------------------------
+// staged fields (each nxx*2L floats, in the (ix, c) walk order):
+//   0 div, 1 Lz, 2 p, 3 c1, 4 c2, 5 psi_px, 6 vx, 7 bbx, 8 psi_vx
 __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
@@ -92,12 +129,50 @@ __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
     const int L = a.L, ld = a.pl.m, nzz = a.nzz, nxx = a.nxx;
     const XTile T(L, blockIdx.x, nzz, nxx);
     float* sf = reinterpret_cast<float*>(smem);
+    float* stg = reinterpret_cast<float*>(smem + (size_t)L * ld);
+    const size_t fstride = (size_t)T.tot;
+    auto S = [&](int f, int g) -> float& { return stg[f * fstride + g]; };
+    if (a.stage) {
+        for (int g = T.t0; g < T.tot; g += T.nthr) {
+            int c, ix;
+            T.split(g, c, ix);
+            const int iz = T.iz0 + c;
+            if (iz >= nzz) continue;
+            const size_t i = (size_t)ix * nzz + iz;
+            if (a.do_p) {
+                cp_async4(&S(1, g), a.Lz + i);
+                cp_async4(&S(2, g), a.p + i);
+                cp_async4(&S(3, g), a.c1 + i);
+                cp_async4(&S(4, g), a.c2 + i);
+            } else if (a.do_v) {
+                cp_async4(&S(2, g), a.p + i);
+            }
+            if (a.do_v) {
+                cp_async4(&S(5, g), a.psi_px + i);
+                cp_async4(&S(6, g), a.vx + i);
+                cp_async4(&S(7, g), a.bbx + i);
+            } else if (a.do_dx) {
+                cp_async4(&S(6, g), a.vx + i);
+            }
+            if (a.do_dx) cp_async4(&S(8, g), a.psi_vx + i);
+        }
+        cp_async_commit();
+    }
 
     bool have = false;  // smem holds the packed field for the next transform
     if (a.do_p) {
-        xload(a.div, sf, T, ld);
+        // div feeds the first transform now and the p update later
+        for (int g = T.t0; g < T.tot; g += T.nthr) {
+            int c, ix;
+            T.split(g, c, ix);
+            const int iz = T.iz0 + c;
+            const float v = (iz < nzz) ? a.div[(size_t)ix * nzz + iz] : 0.f;
+            sf[T.sidx(c, ix, ld)] = v;
+            if (a.stage) S(0, g) = v;
+        }
         __syncthreads();
         roundtrip_conv(smem, ld, fc, L, a.kx2);
+        if (a.stage) cp_async_wait_all();
         for (int g = T.t0; g < T.tot; g += T.nthr) {
             int c, ix;
             T.split(g, c, ix);
@@ -105,8 +180,13 @@ __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
             float pn = 0.f;
             if (iz < nzz) {
                 const size_t i = (size_t)ix * nzz + iz;
-                const float lap = sf[T.sidx(c, ix, ld)] + a.Lz[i];
-                pn = a.p[i] + a.c1[i] * (a.div[i] - a.c2[i] * lap);
+                const float lz = a.stage ? S(1, g) : a.Lz[i];
+                const float p0 = a.stage ? S(2, g) : a.p[i];
+                const float c1 = a.stage ? S(3, g) : a.c1[i];
+                const float c2 = a.stage ? S(4, g) : a.c2[i];
+                const float dv = a.stage ? S(0, g) : a.div[i];
+                const float lap = sf[T.sidx(c, ix, ld)] + lz;
+                pn = p0 + c1 * (dv - c2 * lap);
                 if (ix == a.xs && iz == a.zs) pn += a.src;
             }
             sf[T.sidx(c, ix, ld)] = pn;
@@ -141,9 +221,18 @@ __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
         have = true;
     }
     if (a.do_v) {
-        if (!have) xload(a.p, sf, T, ld);
+        if (!have) {
+            if (a.stage) cp_async_wait_all();
+            for (int g = T.t0; g < T.tot; g += T.nthr) {
+                int c, ix;
+                T.split(g, c, ix);
+                const int iz = T.iz0 + c;
+                sf[T.sidx(c, ix, ld)] = (iz < nzz) ? (a.stage ? S(2, g) : a.p[(size_t)ix * nzz + iz]) : 0.f;
+            }
+        }
         __syncthreads();
         roundtrip_conv(smem, ld, fc, L, a.HxP);
+        if (a.stage) cp_async_wait_all();
         for (int g = T.t0; g < T.tot; g += T.nthr) {
             int c, ix;
             T.split(g, c, ix);
@@ -152,9 +241,12 @@ __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
             if (iz < nzz) {
                 const size_t i = (size_t)ix * nzz + iz;
                 const float d = sf[T.sidx(c, ix, ld)];
-                const float ps = a.h_bx[ix] * a.psi_px[i] + a.h_ax[ix] * d;
+                const float pp = a.stage ? S(5, g) : a.psi_px[i];
+                const float v0 = a.stage ? S(6, g) : a.vx[i];
+                const float bb = a.stage ? S(7, g) : a.bbx[i];
+                const float ps = a.h_bx[ix] * pp + a.h_ax[ix] * d;
                 a.psi_px[i] = ps;
-                nv = a.vx[i] + a.dt * a.bbx[i] * (d + ps);
+                nv = v0 + a.dt * bb * (d + ps);
                 a.vx[i] = nv;
             }
             sf[T.sidx(c, ix, ld)] = nv;
@@ -164,9 +256,18 @@ __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
         have = false;
     }
     if (a.do_dx) {
-        if (!have) xload(a.vx, sf, T, ld);
+        if (!have) {
+            if (a.stage) cp_async_wait_all();
+            for (int g = T.t0; g < T.tot; g += T.nthr) {
+                int c, ix;
+                T.split(g, c, ix);
+                const int iz = T.iz0 + c;
+                sf[T.sidx(c, ix, ld)] = (iz < nzz) ? (a.stage ? S(6, g) : a.vx[(size_t)ix * nzz + iz]) : 0.f;
+            }
+        }
         __syncthreads();
         roundtrip_conv(smem, ld, fc, L, a.HxM);
+        if (a.stage) cp_async_wait_all();
         for (int g = T.t0; g < T.tot; g += T.nthr) {
             int c, ix;
             T.split(g, c, ix);
@@ -174,28 +275,35 @@ __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
             if (iz >= nzz) continue;
             const size_t i = (size_t)ix * nzz + iz;
             const float d = sf[T.sidx(c, ix, ld)];
-            const float ps = a.i_bx[ix] * a.psi_vx[i] + a.i_ax[ix] * d;
+            const float pv = a.stage ? S(8, g) : a.psi_vx[i];
+            const float ps = a.i_bx[ix] * pv + a.i_ax[ix] * d;
             a.psi_vx[i] = ps;
             a.Dx[i] = d + ps;
         }
     }
 }
 
+size_t ac_zpass_smem(int L, int m, int nzz, bool stage) {
+    return sizeof(float2) * (size_t)L * m + (stage ? sizeof(float) * 5 * (size_t)L * 2 * nzz : 0);
+}
+size_t ac_xpass_smem(int L, int m, int nxx, bool stage) {
+    return sizeof(float2) * (size_t)L * m + (stage ? sizeof(float) * 9 * (size_t)nxx * 2 * L : 0);
+}
+
 void launch_ac_zpass(const AcZArgs& a, cudaStream_t s) {
     const int grid = (a.nxx + 2 * a.L - 1) / (2 * a.L);
-    const size_t sm = sizeof(float2) * (size_t)a.L * a.pl.m;
-    ac_zpass_kernel<<<grid, dim3(a.pl.tx, a.L), sm, s>>>(a);
+    ac_zpass_kernel<<<grid, dim3(a.pl.tx, a.L), ac_zpass_smem(a.L, a.pl.m, a.nzz, a.stage), s>>>(a);
 }
 
 void launch_ac_xpass(const AcXArgs& a, cudaStream_t s) {
     const int grid = (a.nzz + 2 * a.L - 1) / (2 * a.L);
-    const size_t sm = sizeof(float2) * (size_t)a.L * a.pl.m;
-    ac_xpass_kernel<<<grid, dim3(a.pl.tx, a.L), sm, s>>>(a);
+    ac_xpass_kernel<<<grid, dim3(a.pl.tx, a.L), ac_xpass_smem(a.L, a.pl.m, a.nxx, a.stage), s>>>(a);
 }
 
 int ac_set_smem_limits() {
-    cudaError_t e1 = cudaFuncSetAttribute(ac_zpass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaError_t e2 = cudaFuncSetAttribute(ac_xpass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    const int lim = QP_SMEM_DYN_MAX;
+    cudaError_t e1 = cudaFuncSetAttribute(ac_zpass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaError_t e2 = cudaFuncSetAttribute(ac_xpass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     return (e1 == cudaSuccess && e2 == cudaSuccess) ? 0 : -1;
 }
 

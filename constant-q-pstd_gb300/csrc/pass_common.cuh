@@ -6,6 +6,17 @@
 
 namespace qp {
 
+// Asynchronous 4-byte global->shared copies (cp.async, completion per thread).
+// A pass stages the inputs of its epilogues at kernel start so their loads
+// overlap the FFT work; every thread later reads back only the elements it
+// staged itself, so a per-thread wait (no barrier) suffices.
+__device__ __forceinline__ void cp_async4(float* sdst, const float* gsrc) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // Compensated accumulation s += v (Kahan), used for the image and the
 // illumination sums over thousands of steps.
 __device__ __forceinline__ void kahan_add(float* s, float* c, size_t i, float v) {

@@ -6,6 +6,9 @@
 // Threads per CTA of the pass kernels (__launch_bounds__(QP_MAXTHREADS, 1):
 // 80 registers per thread, enough for the radix-16 butterflies).
 #define QP_MAXTHREADS 768
+// Dynamic shared memory a pass kernel may request: the 227 KB per-CTA opt-in
+// minus the static plan copies.
+#define QP_SMEM_DYN_MAX (232448 - 1024)
 
 namespace qp {
 
@@ -57,6 +60,7 @@ struct AcZArgs {
     float *div, *Lz;
     float dt;
     int do_v, do_div;
+    int stage;                    // stage epilogue inputs in shared memory (cp.async)
 };
 
 // ---------------------------------------------------------------------------
@@ -87,6 +91,7 @@ struct AcXArgs {
     float *ssg, *ssg_c;           // illumination accumulation, Kahan pair (NULL: off)
     float *img, *img_c;           // image accumulation, Kahan pair (NULL: off)
     const float* ps;              // source wavefield p for imaging
+    int stage;                    // stage epilogue inputs in shared memory (cp.async)
 };
 
 // ---------------------------------------------------------------------------

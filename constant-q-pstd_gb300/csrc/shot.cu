@@ -93,8 +93,10 @@ static int upload_plan(qpstd_shot* s, const HostPlan& hp, FFTPlanDev& d) {
 // Complex lines per CTA: bounded by the CTA's threads (tx per line), by shared
 // memory (nbuf line buffers of m float2), and small enough that the grid
 // covers the 152 SMs about twice.  pow2: x tiles need a power of two.
-static int choose_L(int nlines, int m, int tx, int nbuf, bool pow2) {
-    const int lmax = std::max(1, std::min(QP_MAXTHREADS / tx, (int)((160 * 1024) / ((size_t)8 * m * nbuf))));
+static int choose_L(int nlines, int m, int tx, int nbuf, bool pow2, size_t extra_per_line = 0,
+                    size_t budget = 160 * 1024) {
+    const size_t per_line = (size_t)8 * m * nbuf + extra_per_line;
+    const int lmax = std::max(1, std::min(QP_MAXTHREADS / tx, (int)(budget / per_line)));
     int L = (nlines + 2 * 152 - 1) / (2 * 152);
     L = std::max(1, std::min(L, lmax));
     if (pow2) {
@@ -410,8 +412,15 @@ extern "C" int qpstd_shot_create(const qpstd_shot_desc* d, qpstd_shot** out) {
         if ((rc = upload_plan(s, hz, s->pz))) return bail(rc);
         if ((rc = setup_conv(s, d))) return bail(rc);
         const int pairs_z = (nxx + 1) / 2, pairs_x = (nzz + 1) / 2;
-        s->Lx = choose_L(pairs_x, s->pxc.m, s->pxc.tx, 1, true);
-        s->Lzp = choose_L(pairs_z, s->pzc.m, s->pzc.tx, 1, false);
+        // acoustic passes: stage the epilogue inputs when they fit beside the lines
+        // (z: 5 fields x 2 rows x nzz floats per line; x: 9 fields x 2 columns x nxx)
+        const size_t stz = (size_t)40 * nzz, stx = (size_t)72 * nxx;
+        s->stage_z = ((size_t)8 * s->pzc.m + stz) <= (size_t)QP_SMEM_DYN_MAX;
+        s->stage_x = ((size_t)8 * s->pxc.m + stx) <= (size_t)QP_SMEM_DYN_MAX;
+        s->Lx = choose_L(pairs_x, s->pxc.m, s->pxc.tx, 1, true, s->stage_x ? stx : 0,
+                         s->stage_x ? (size_t)QP_SMEM_DYN_MAX : 160 * 1024);
+        s->Lzp = choose_L(pairs_z, s->pzc.m, s->pzc.tx, 1, false, s->stage_z ? stz : 0, 110 * 1024);
+        if (s->stage_z && (size_t)8 * s->pzc.m + stz > 110 * 1024) s->Lzp = 1;
         // constant-Q: z pass B and the 3-output x-spectral pass hold two line buffers;
         // z pass A uses both the exact and the convolution plan
         s->Lzv = choose_L(pairs_z, std::max(s->pz.m, s->pzc.m), std::max(s->pz.tx, s->pzc.tx), 2, false);
@@ -528,6 +537,7 @@ static AcZArgs zargs(qpstd_shot* s, Wave& w, int do_v, int do_div) {
     a.dt = s->d.dt;
     a.do_v = do_v;
     a.do_div = do_div;
+    a.stage = s->stage_z ? 1 : 0;
     return a;
 }
 
@@ -562,6 +572,7 @@ static AcXArgs xargs(qpstd_shot* s, Wave& w, int do_p, int do_v, int do_dx) {
     a.do_dx = do_dx;
     a.xs = -1;
     a.zs = -1;
+    a.stage = s->stage_x ? 1 : 0;
     return a;
 }
 

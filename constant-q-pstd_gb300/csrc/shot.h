@@ -52,6 +52,7 @@ struct qpstd_shot {
     const float2 *cHxM = nullptr, *cHxP = nullptr, *cKx2 = nullptr;  // convolution multipliers
     const float2 *cHzM = nullptr, *cHzP = nullptr, *cKz2 = nullptr;
     int Lx = 1, Lzp = 1, ntile_x = 0;
+    bool stage_x = false, stage_z = false;  // acoustic passes stage epilogue inputs
     int* rec_off = nullptr;
     qp::RecEntry* rec = nullptr;
     // constant-Q step
