@@ -876,8 +876,11 @@ extern "C" int qpstd_shot_set_obs(qpstd_shot* s, const float* obs) {
 }
 
 // Revolve-driven RTM, the action loop of sgpstd-qrtm/acps4.cu:449-905 and
-// sgpstd-qrtm/acsglw.cu:470-1039.
-extern "C" int qpstd_shot_rtm_device(qpstd_shot* s) {
+// sgpstd-qrtm/acsglw.cu:470-1039, as a resumable state machine: rtm_begin()
+// resets the shot, each rtm_action() enqueues one revolve action on the
+// shot's stream and returns 1 once revolve terminates.  A batch interleaves
+// the actions of its shots, so their work overlaps on the device.
+int rtm_begin(qpstd_shot* s) {
     if (!s || !s->rtm) return fail(QPSTD_EINVAL, "not an RTM shot");
     const size_t N = s->N, NI = (size_t)s->nx * s->nz;
     cudaStream_t st = s->stream;
@@ -887,46 +890,81 @@ extern "C" int qpstd_shot_rtm_device(qpstd_shot* s) {
     CK(cudaMemsetAsync(s->rcv.st, 0, sizeof(float) * 9 * N, st));
     CK(cudaMemsetAsync(s->img, 0, sizeof(float) * 4 * NI, st));
     s->src.aux_pending = s->rcv.aux_pending = false;
-    Revolve rv(s->d.nt, s->d.snaps);
-    int ts = 0, rc;
-    bool first_sweep = true, first_rcv = true;
-    for (;;) {
-        const RevolveAction act = rv.next();
-        if (act == RV_TAKESHOT) {
-            float* slot = s->store + (size_t)rv.check() * 8 * N;
-            CK(cudaMemcpyAsync(slot, s->src.st, sizeof(float) * 8 * N, cudaMemcpyDeviceToDevice, st));
-            if (rv.capo() == 0) {
-                // checkpoint 0 also holds the first source sample (acsglw.cu:493-500)
-                ProfScope ps(s, QPSTD_K_OTHER);
-                add_point_kernel<<<1, 1, 0, st>>>(slot + (size_t)s->d.xsg * s->d.nzz + s->d.zsg,
-                                                  (float)((double)s->rik[0] * 1000.0 * s->d.dt));
-            }
-        } else if (act == RV_ADVANCE) {
-            const int n = rv.capo() - ts + 1;
-            if ((rc = advance_src(s, ts, n, nullptr, first_sweep))) return rc;
-            s->fwd_steps += n;
-            ts = rv.capo() + 1;
-        } else if (act == RV_FIRSTURN || act == RV_YOUTURN) {
-            if (act == RV_FIRSTURN) first_sweep = false;
-            const int row = (act == RV_FIRSTURN) ? s->d.nt - 1 : rv.capo();
-            if ((rc = receiver_step(s, row, first_rcv))) return rc;
-            first_rcv = false;
-        } else if (act == RV_RESTORE) {
-            const float* slot = s->store + (size_t)rv.check() * 8 * N;
-            CK(cudaMemcpyAsync(s->src.st, slot, sizeof(float) * 8 * N, cudaMemcpyDeviceToDevice, st));
-            s->src.aux_pending = false;
-            ts = rv.capo() + 1;
-        } else if (act == RV_TERMINATE) {
-            break;
-        } else {
-            char buf[96];
-            snprintf(buf, sizeof(buf), "irregular termination of revolve (info %d)", rv.info());
-            return fail(QPSTD_EREVOLVE, buf);
-        }
-    }
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    s->run = RtmRun();
+    s->run.rv = Revolve(s->d.nt, s->d.snaps);
     return QPSTD_OK;
+}
+
+int rtm_action(qpstd_shot* s) {
+    RtmRun& r = s->run;
+    if (r.done) return 1;
+    const size_t N = s->N;
+    cudaStream_t st = s->stream;
+    int rc;
+    if (r.adv_left > 0) {
+        // continue an advance in slices so that the shots of a batch interleave
+        const int n = std::min(r.adv_left, r.slice);
+        for (int i = 0; i < n; i++) {
+            const int t = r.adv_t++;
+            src_step(s, t, t == r.adv_t0, r.adv_left == 1, nullptr, r.first_sweep);
+            r.adv_left--;
+        }
+        if (r.adv_left == 0) src_end(s);
+        if (s->plain_err) return fail(QPSTD_ECUDA, "plain step failed (cuFFT or launch)");
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+        return 0;
+    }
+    const RevolveAction act = r.rv.next();
+    if (act == RV_TAKESHOT) {
+        float* slot = s->store + (size_t)r.rv.check() * 8 * N;
+        CK(cudaMemcpyAsync(slot, s->src.st, sizeof(float) * 8 * N, cudaMemcpyDeviceToDevice, st));
+        if (r.rv.capo() == 0) {
+            // checkpoint 0 also holds the first source sample (acsglw.cu:493-500)
+            ProfScope ps(s, QPSTD_K_OTHER);
+            add_point_kernel<<<1, 1, 0, st>>>(slot + (size_t)s->d.xsg * s->d.nzz + s->d.zsg,
+                                              (float)((double)s->rik[0] * 1000.0 * s->d.dt));
+        }
+    } else if (act == RV_ADVANCE) {
+        const int n = r.rv.capo() - r.ts + 1;
+        s->fwd_steps += n;
+        if (r.slice >= n) {
+            if ((rc = advance_src(s, r.ts, n, nullptr, r.first_sweep))) return rc;
+        } else if (n > 0) {
+            src_begin(s);
+            r.adv_t0 = r.adv_t = r.ts;
+            r.adv_left = n;
+        }
+        r.ts = r.rv.capo() + 1;
+    } else if (act == RV_FIRSTURN || act == RV_YOUTURN) {
+        if (act == RV_FIRSTURN) r.first_sweep = false;
+        const int row = (act == RV_FIRSTURN) ? s->d.nt - 1 : r.rv.capo();
+        if ((rc = receiver_step(s, row, r.first_rcv))) return rc;
+        r.first_rcv = false;
+    } else if (act == RV_RESTORE) {
+        const float* slot = s->store + (size_t)r.rv.check() * 8 * N;
+        CK(cudaMemcpyAsync(s->src.st, slot, sizeof(float) * 8 * N, cudaMemcpyDeviceToDevice, st));
+        s->src.aux_pending = false;
+        r.ts = r.rv.capo() + 1;
+    } else if (act == RV_TERMINATE) {
+        r.done = true;
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+        return 1;
+    } else {
+        char buf[96];
+        snprintf(buf, sizeof(buf), "irregular termination of revolve (info %d)", r.rv.info());
+        return fail(QPSTD_EREVOLVE, buf);
+    }
+    return 0;
+}
+
+extern "C" int qpstd_shot_rtm_device(qpstd_shot* s) {
+    int rc = rtm_begin(s);
+    if (rc) return rc;
+    while ((rc = rtm_action(s)) == 0) {
+    }
+    return rc < 0 ? rc : QPSTD_OK;
 }
 
 extern "C" int qpstd_shot_get_image(qpstd_shot* s, float* img, float* ssg) {

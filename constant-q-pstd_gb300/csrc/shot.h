@@ -7,6 +7,7 @@
 #include "../../include/qpstd.h"
 #include "plain.h"
 #include "qpstd_internal.h"
+#include "revolve.h"
 
 namespace qp {
 
@@ -31,9 +32,23 @@ struct Wave {
     bool aux_pending = false;
 };
 
+// Progress of one shot's revolve-driven RTM.
+struct RtmRun {
+    Revolve rv{1, 1};
+    int ts = 0;
+    bool first_sweep = true, first_rcv = true, done = false;
+    int slice = 1 << 30;            // steps of an advance enqueued per action call
+    int adv_t0 = 0, adv_t = 0, adv_left = 0;
+};
+
 }  // namespace qp
 
+struct qpstd_shot;
+int rtm_begin(qpstd_shot* s);
+int rtm_action(qpstd_shot* s);  // 0: more actions, 1: finished, < 0: error code
+
 struct qpstd_shot {
+    qp::RtmRun run;
     qpstd_shot_desc d{};
     size_t N = 0;
     int nx = 0, nz = 0;

@@ -74,6 +74,16 @@ EXPORTS = {
     "qpstd_shot_pipeline_end": (C.c_int, [C.c_void_p]),
     "qpstd_shot_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "qpstd_shot_profile_read": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
+    "qpstd_batch_create": (C.c_int, [C.POINTER(ShotDesc), C.c_int, C.POINTER(C.c_void_p)]),
+    "qpstd_batch_destroy": (C.c_int, [C.c_void_p]),
+    "qpstd_batch_size": (C.c_int, [C.c_void_p]),
+    "qpstd_batch_shot": (C.c_void_p, [C.c_void_p, C.c_int]),
+    "qpstd_batch_sync": (C.c_int, [C.c_void_p]),
+    "qpstd_batch_rtm_device": (C.c_int, [C.c_void_p, C.c_int]),
+    "qpstd_batch_pipeline_begin": (C.c_int, [C.c_void_p]),
+    "qpstd_batch_pipeline_step": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "qpstd_batch_pipeline_end": (C.c_int, [C.c_void_p]),
+    "qpstd_rtm_batch": (C.c_int, [C.POINTER(ShotDesc), C.c_int, C.POINTER(_fp), C.POINTER(_fp), C.POINTER(_fp)]),
 }
 KIND_NAMES = ["xpass", "zpass", "xspec", "other", "plain"]
 
@@ -236,3 +246,78 @@ class Shot:
         cnt = (C.c_longlong * n)()
         _check(lib().qpstd_shot_profile_read(self.h, n, ms, cnt))
         return {KIND_NAMES[k]: (ms[k], cnt[k]) for k in range(n)}
+
+
+class Batch:
+    """Several resident shots advancing together (qpstd_batch handle)."""
+
+    def __init__(self, dicts, method: int = FUSED):
+        self.D = [Desc(d, method) for d in dicts]
+        arr = (ShotDesc * len(dicts))(*[x.s for x in self.D])
+        self._arr = arr
+        self.h = C.c_void_p()
+        _check(lib().qpstd_batch_create(arr, len(dicts), C.byref(self.h)))
+        self.dicts = dicts
+
+    def close(self):
+        if self.h:
+            lib().qpstd_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def shot(self, i: int):
+        return C.c_void_p(lib().qpstd_batch_shot(self.h, i))
+
+    def set_obs(self, i: int, obs):
+        obs = np.ascontiguousarray(obs, dtype=np.float32)
+        setattr(self, f"_obs{i}", obs)
+        _check(lib().qpstd_shot_set_obs(self.shot(i), _f(obs)))
+
+    def rtm_device(self, slice_steps: int = 8):
+        _check(lib().qpstd_batch_rtm_device(self.h, slice_steps))
+
+    def get_image(self, i: int):
+        d = self.dicts[i]
+        nx, nz = d["nxx"] - 2 * d["pml"], d["nzz"] - 2 * d["pml"]
+        img = np.zeros((nx, nz), dtype=np.float32)
+        ssg = np.zeros((nx, nz), dtype=np.float32)
+        _check(lib().qpstd_shot_get_image(self.shot(i), _f(img), _f(ssg)))
+        return img, ssg
+
+    def sync(self):
+        _check(lib().qpstd_batch_sync(self.h))
+
+    def pipeline_begin(self):
+        _check(lib().qpstd_batch_pipeline_begin(self.h))
+
+    def pipeline_step(self, t: int, last: bool = False):
+        _check(lib().qpstd_batch_pipeline_step(self.h, t, 1 if last else 0))
+
+    def pipeline_end(self):
+        _check(lib().qpstd_batch_pipeline_end(self.h))
+
+    def stream_ptrs(self):
+        return [int(lib().qpstd_shot_stream(self.shot(i)) or 0) for i in range(len(self.dicts))]
+
+
+def rtm_batch(dicts, obs_list, method: int = FUSED):
+    """One call with host buffers: concurrent RTM of several shots."""
+    D = [Desc(d, method) for d in dicts]
+    arr = (ShotDesc * len(dicts))(*[x.s for x in D])
+    obs = [np.ascontiguousarray(o, dtype=np.float32) for o in obs_list]
+    imgs, ssgs = [], []
+    for d in dicts:
+        nx, nz = d["nxx"] - 2 * d["pml"], d["nzz"] - 2 * d["pml"]
+        imgs.append(np.zeros((nx, nz), dtype=np.float32))
+        ssgs.append(np.zeros((nx, nz), dtype=np.float32))
+    po = (_fp * len(obs))(*[_f(o) for o in obs])
+    pi = (_fp * len(imgs))(*[_f(a) for a in imgs])
+    ps = (_fp * len(ssgs))(*[_f(a) for a in ssgs])
+    _check(lib().qpstd_rtm_batch(arr, len(dicts), po, pi, ps))
+    return imgs, ssgs
+

@@ -148,6 +148,36 @@ def window_shot(models: dict, xs, zs, gxp, gzp, pml, dx, dz, sroffmx, disx=0.0):
     return out, nx, nz, xsg, zsg, gxg, gzg
 
 
+def parent_model(nx: int, nz: int, seed: int, nlayers: int = 12, nanom: int = 3, fd: float = 20.0,
+                 fo: float = 20.0, dx: float = 10.0):
+    """A seeded parent model (vp, rho, Q and the derived fields) for batches."""
+    vp, qp = layered_model(nx, nz, nlayers, nanom, seed, dx=dx, sigma_cells=15.0)
+    rho = gardner(vp)
+    bbx, bbz = bbx_bbz(rho)
+    gam, lam, vwd, tao = transfermodel(fd, fo, vp, qp)
+    return {"vp": vp, "rho": rho, "bbx": bbx, "bbz": bbz, "gam": gam, "lam": lam, "vwd": vwd, "tao": tao}
+
+
+def window_of_parent(kind: int, parent: dict, x0: int, nx: int, pml: int, nt: int, dt: float, fd: float,
+                     snaps: int, dx: float = 10.0, dz: float = 10.0):
+    """One shot whose window is columns [x0, x0+nx) of the parent model: the
+    source at the window centre and z = 2 cells, a receiver in every window
+    column at z = 2 cells, the window padded by expand_pml_areas."""
+    nz = parent["vp"].shape[1]
+    nxx, nzz = nx + 2 * pml, nz + 2 * pml
+    d = dict(kind=kind, nxx=nxx, nzz=nzz, pml=pml, dx=dx, dz=dz, dt=dt, fd=fd, nt=nt,
+             rik=ricker(nt, dt, fd, 2), xsg=pml + nx // 2, zsg=pml + 2,
+             gxg=np.arange(pml, pml + nx, dtype=np.int32), gzg=np.full(nx, pml + 2, dtype=np.int32),
+             snaps=snaps, etas=1e-20, etar=1e-20)
+    for k, full in parent.items():
+        a = np.zeros((nxx, nzz))
+        a[pml:pml + nx, pml:pml + nz] = full[x0:x0 + nx, :]
+        d[k] = expand_pml_areas(a, pml).ravel()
+    if "tao" in parent:
+        d["taoc"] = float(d["tao"].max())
+    return d
+
+
 def make_shot(kind: int, nx_model: int, nz_model: int, pml: int, nt: int, dt: float, fd: float,
               seed: int, nlayers: int = 5, nanom: int = 1, fo: float = 20.0, snaps: int = 20,
               xs_cells: int | None = None, dx: float = 10.0, dz: float = 10.0,

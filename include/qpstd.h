@@ -134,6 +134,28 @@ void *qpstd_shot_stream(qpstd_shot *s);
 int qpstd_shot_set_profiling(qpstd_shot *s, int on);
 int qpstd_shot_profile_read(qpstd_shot *s, int nkinds, double *ms, long long *count);
 
+/* ---- batches: many resident shots advancing together ---------------------
+ * The reference runs a rank's shots one after another (the shot loop of
+ * acforward, sgpstd-qrtm/acsglw.cu:304).  A batch keeps all of them in HBM,
+ * each with its own stream, and interleaves their revolve actions so their
+ * kernels overlap.  Windows (nxx), nt and snaps may differ between shots. */
+typedef struct qpstd_batch qpstd_batch;
+int qpstd_batch_create(const qpstd_shot_desc *d, int nshots, qpstd_batch **out);
+int qpstd_batch_destroy(qpstd_batch *b);
+int qpstd_batch_size(const qpstd_batch *b);
+/* The i-th shot (for qpstd_shot_set_obs / get_image / get_state ...). */
+qpstd_shot *qpstd_batch_shot(qpstd_batch *b, int i);
+int qpstd_batch_sync(qpstd_batch *b);
+/* RTM of every shot; advances are enqueued `slice` steps at a time per shot. */
+int qpstd_batch_rtm_device(qpstd_batch *b, int slice);
+int qpstd_batch_pipeline_begin(qpstd_batch *b);
+int qpstd_batch_pipeline_step(qpstd_batch *b, int t, int last);
+int qpstd_batch_pipeline_end(qpstd_batch *b);
+/* One call with host buffers: obs[i] nt*nr, img[i] and ssg[i] nx*nz of shot i
+ * (ssg may be NULL). */
+int qpstd_rtm_batch(const qpstd_shot_desc *d, int nshots, const float *const *obs, float *const *img,
+                    float *const *ssg);
+
 #ifdef __cplusplus
 }
 #endif
