@@ -51,6 +51,9 @@ static int cuda_fail(cudaError_t e, const char* where) {
     } while (0)
 
 extern "C" const char* qpstd_last_error(void) { return g_err.c_str(); }
+namespace qp {
+void set_last_error(const std::string& m) { g_err = m; }
+}  // namespace qp
 extern "C" int qpstd_version(void) { return 100; }
 
 // ---------------------------------------------------------------------------

@@ -84,6 +84,8 @@ EXPORTS = {
     "qpstd_batch_pipeline_step": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "qpstd_batch_pipeline_end": (C.c_int, [C.c_void_p]),
     "qpstd_rtm_batch": (C.c_int, [C.POINTER(ShotDesc), C.c_int, C.POINTER(_fp), C.POINTER(_fp), C.POINTER(_fp)]),
+    "qpstd_ac_advance_noalloc": (C.c_int, [C.POINTER(ShotDesc)] + [C.c_void_p] * 5
+                                 + [C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
 }
 KIND_NAMES = ["xpass", "zpass", "xspec", "other", "plain"]
 

@@ -156,6 +156,28 @@ int qpstd_batch_pipeline_end(qpstd_batch *b);
 int qpstd_rtm_batch(const qpstd_shot_desc *d, int nshots, const float *const *obs, float *const *img,
                     float *const *ssg);
 
+/* ---- acoustic steps without device allocation ---------------------------
+ * No counterpart in the reference (its acforward allocates all device memory
+ * itself).  For callers that cannot call cudaMalloc -- code running while
+ * another part of the process captures a CUDA graph, plug-ins that may only
+ * use the buffers their host hands them, hosts whose device memory belongs to
+ * a pool they do not own.  Runs nsteps acoustic steps (aps / the source side of
+ * artm) from step index t0, exactly as qpstd_shot_advance does, with every
+ * scratch buffer and table in a static array of QPSTD_NOALLOC_FLOATS floats
+ * (24 MiB) that each GPU loading the library keeps until exit; grids above
+ * QPSTD_NOALLOC_MAX_POINTS points are rejected with QPSTD_EINVAL.
+ * d: the shot (scalars, wavelet and receivers on the host; its model pointers
+ *    are not read); vp, rho, bbx, bbz: device, nxx*nzz each; state: device,
+ *    8*nxx*nzz (p, vx, vz, fipx, fipz, fivxx, fivzz, aux), advanced in place;
+ *    gather: device nsteps*nr or NULL; stream: a cudaStream_t (NULL: legacy).
+ * The first call on a device looks up the array's address (make it before any
+ * stream capture).  Calls share the array: calls that overlap on the GPU race
+ * and must be serialised by the caller. */
+#define QPSTD_NOALLOC_FLOATS (6 * 1024 * 1024)
+#define QPSTD_NOALLOC_MAX_POINTS (1024 * 1024)
+int qpstd_ac_advance_noalloc(const qpstd_shot_desc *d, const float *vp, const float *rho, const float *bbx,
+                             const float *bbz, float *state, int t0, int nsteps, float *gather, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
