@@ -125,13 +125,26 @@ struct VzArgsA {
 //   mode 2: one output with the Q-RTM stabilised symbol at time t_filter
 struct VxsArgs {
     int nxx, nzz, nzh, L, mode;
-    FFTPlanDev pl;
+    FFTPlanDev pl;            // exact length-nxx DFT plan (mode 2)
+    FFTPlanDev plc;           // convolution plan along x (modes 0, 1)
     const float *kx2, *kz2;   // squared wavenumbers (unnormalised)
     const float2* in;
     float2 *out0, *out1, *out2;
+    const float *tab0, *tab1, *tab2;  // per-kz convolution multipliers, nzh x plc.m (modes 0, 1)
     float norm;               // 1/(nxx*nzz)
     float eta6;               // eta * 1e-6 (mode 2)
     float tao, dt, tt;        // filter tau, dt, nt*dt (mode 2)
+};
+
+// Builds the per-kz convolution multipliers of a stationary 2-D symbol:
+// for each kz, h = norm * IDFT_x(sym(kx, kz)) zero-padded and wrapped to
+// plc.m, then out[kz*plc.m + k] = Re FFT_m(h)[k] / m.
+struct VtabArgs {
+    int nxx, nzz, nzh, L, sym;  // sym: 0 (k^2)^(1/32), 1 k^2, 2 (k^2)^(33/32), 3 (k^2)^0.505
+    FFTPlanDev pl, plc;
+    const float *kx2, *kz2;
+    float norm;
+    float* out;
 };
 
 // z pass B: Y2, Y3, Y4 from their spectra; total; total -> half spectrum T.

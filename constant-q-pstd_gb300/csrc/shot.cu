@@ -29,6 +29,8 @@ void launch_vz_xspec(const VxsArgs& a, cudaStream_t s);
 void launch_vz_passB(const VzArgsB& a, cudaStream_t s);
 void launch_vz_passC(const VzArgsC& a, cudaStream_t s);
 void launch_vz_zinv(const VzArgsI& a, cudaStream_t s);
+void launch_vz_xspec_conv(const VxsArgs& a, cudaStream_t s);
+void launch_vz_convtab(const VtabArgs& a, cudaStream_t s);
 int vz_set_smem_limits();
 }  // namespace qp
 
@@ -243,6 +245,38 @@ static int setup_ksq(qpstd_shot* s, const qpstd_shot_desc* d) {
     return QPSTD_OK;
 }
 
+// Convolution tables of the stationary constant-Q symbols.  When nxx is not a
+// smooth length the exact x transforms of the x-spectral passes go through
+// Bluestein (two FFTs each); a symbol that does not change in time is instead
+// applied per kz column as a circular convolution along x on the smooth
+// convolution length (one FFT per output after a shared forward FFT).
+static int setup_xtabs(qpstd_shot* s, const qpstd_shot_desc* d) {
+    if (!s->px.blue) return QPSTD_OK;
+    int rc = QPSTD_OK;
+    const int mc = s->pxc.m, nzh = s->nzh;
+    float* t = dalloc(s, (size_t)4 * nzh * mc, &rc);
+    if (!t) return rc;
+    VtabArgs a{};
+    a.nxx = d->nxx; a.nzz = d->nzz; a.nzh = nzh;
+    a.pl = s->px; a.plc = s->pxc; a.kx2 = s->kxsq; a.kz2 = s->kzsq;
+    a.norm = (float)(1.0 / ((double)d->nxx * d->nzz));
+    a.L = choose_L(nzh, std::max(s->px.m, mc), std::max(s->px.tx, s->pxc.tx), 1, false);
+    for (int k = 0; k < 4; k++) {
+        a.sym = k;
+        a.out = t + (size_t)k * nzh * mc;
+        s->xtab[k] = a.out;
+        launch_vz_convtab(a, s->stream);
+    }
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "convolution tables");
+    s->xconv = true;
+    s->Lxs_exact = s->Lxs;
+    s->Lxs = choose_L(nzh, mc, s->pxc.tx, 1, true);
+    s->Lxs3 = choose_L(nzh, mc, s->pxc.tx, 2, true);
+    return QPSTD_OK;
+}
+
 // Plain form: cuFFT plan, scratch, and the reference's own shift symbols.
 static int setup_plain(qpstd_shot* s, const qpstd_shot_desc* d) {
     std::string err;
@@ -434,6 +468,7 @@ extern "C" int qpstd_shot_create(const qpstd_shot_desc* d, qpstd_shot** out) {
     }
     if (s->visco && (rc = setup_visco(s, d))) return bail(rc);
     if ((rc = setup_ksq(s, d))) return bail(rc);
+    if (s->visco && (rc = setup_xtabs(s, d))) return bail(rc);
     if (d->method == QPSTD_PLAIN && (rc = setup_plain(s, d))) return bail(rc);
     if ((rc = build_receivers(s, d))) return bail(rc);
     s->gather = dalloc(s, (size_t)d->nt * std::max(d->nr, 1), &rc);
@@ -622,12 +657,24 @@ static void vz_step(qpstd_shot* s, Wave& w, float src, int t_filter, float eta, 
     }
     VxsArgs xs{};
     xs.nxx = nxx; xs.nzz = nzz; xs.nzh = nzh; xs.pl = s->px; xs.kx2 = s->kxsq; xs.kz2 = s->kzsq; xs.norm = norm;
+    xs.plc = s->pxc;
+    // modes 0 and 1 (stationary symbols): per-kz convolution tables when built
+    auto xspec = [&](VxsArgs& a) {
+        if (s->xconv && a.mode != 2) {
+            a.tab0 = s->xtab[a.mode == 0 ? 0 : 3];
+            a.tab1 = s->xtab[1];
+            a.tab2 = s->xtab[2];
+            launch_vz_xspec_conv(a, st);
+        } else {
+            launch_vz_xspec(a, st);
+        }
+    };
     {
         VxsArgs a = xs;
         a.mode = 0; a.L = s->Lxs3;
         a.in = s->spec[0]; a.out0 = s->spec[1]; a.out1 = s->spec[2]; a.out2 = s->spec[3];
         ProfScope ps(s, QPSTD_K_XSPEC);
-        launch_vz_xspec(a, st);
+        xspec(a);
     }
     {
         VzArgsB a{};
@@ -643,7 +690,7 @@ static void vz_step(qpstd_shot* s, Wave& w, float src, int t_filter, float eta, 
         a.mode = 1; a.L = s->Lxs;
         a.in = s->spec[0]; a.out0 = s->spec[1];
         ProfScope ps(s, QPSTD_K_XSPEC);
-        launch_vz_xspec(a, st);
+        xspec(a);
     }
     {
         VzArgsC a{};
@@ -676,8 +723,9 @@ static void vz_step(qpstd_shot* s, Wave& w, float src, int t_filter, float eta, 
         } else {
             a.mode = 1;
         }
+        if (a.mode == 2 && s->xconv) a.L = s->Lxs_exact;
         ProfScope ps(s, QPSTD_K_XSPEC);
-        launch_vz_xspec(a, st);
+        xspec(a);
         w.aux_pending = true;
     }
 }

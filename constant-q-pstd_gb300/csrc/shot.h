@@ -72,12 +72,18 @@ struct qpstd_shot {
     qp::RecEntry* rec = nullptr;
     // constant-Q step
     int nzh = 0, Lzv = 1, Lxs = 1, Lxs3 = 1;
+    int Lxs_exact = 1;                       // exact x-spectral pass (time-dependent filter) when xconv
     float2* spec[4] = {nullptr, nullptr, nullptr, nullptr};
     float* total = nullptr;
     float *y1 = nullptr, *y2 = nullptr, *y3c = nullptr, *y4c = nullptr;
     float *e1 = nullptr, *e2 = nullptr, *e3 = nullptr;
     float *kxsq = nullptr, *kzsq = nullptr;   // unnormalised squared wavenumbers
-    int* rec_off_z = nullptr;                  // receivers keyed by z-pass tile
+    // x-spectral passes with stationary symbols as per-kz convolutions (when
+    // nxx needs Bluestein): tables nzh x pxc.m for (k^2)^(1/32), k^2,
+    // (k^2)^(33/32), (k^2)^0.505
+    bool xconv = false;
+    const float* xtab[4] = {nullptr, nullptr, nullptr, nullptr};
+    int* rec_off_z = nullptr;                // receivers keyed by z-pass tile
     qp::RecEntry* rec_z = nullptr;
     // plain (cuFFT) form
     qp::PlainState plain;

@@ -165,6 +165,92 @@ __global__ void __launch_bounds__(768, 1) vz_xspec_kernel(VxsArgs a) {
     }
 }
 
+// ---- x-spectral pass, stationary symbols as per-kz convolutions ---------------
+// A stationary symbol s(kx, kz) acts on one kz column as a circular
+// convolution along x, so a zero-padded FFT on the smooth convolution length
+// replaces the exact (Bluestein) DFTs: one forward transform, then per output a
+// multiply by the column's table and one inverse transform.
+__global__ void __launch_bounds__(768, 1) vz_xspec_conv_kernel(VxsArgs a) {
+    extern __shared__ float2 smem[];
+    __shared__ FFTPass s_pass[QP_MAXST];
+    const FFTCtx fc = make_ctx(a.plc, s_pass);
+    const int L = a.L, m = a.plc.m, ld = m, nxx = a.nxx, nzh = a.nzh;
+    const int lg = 31 - __clz(L);
+    const int kz0 = blockIdx.x * L;
+    const int t0 = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+    const int tot = L * nxx;
+    const int nout = (a.mode == 0) ? 3 : 1;
+    float2* X = smem + (size_t)L * ld;  // kept forward spectrum (three-output mode)
+    float2* line = smem + threadIdx.y * ld;
+    for (int g = t0; g < tot; g += nthr) {
+        const int c = g & (L - 1), ix = g >> lg;
+        const int kz = kz0 + c;
+        smem[c * ld + ix] = (kz < nzh) ? a.in[(size_t)ix * nzh + kz] : make_float2(0.f, 0.f);
+    }
+    for (int k = nxx + threadIdx.x; k < m; k += blockDim.x) line[k] = make_float2(0.f, 0.f);
+    __syncthreads();
+    fft_m<-1>(smem, ld, fc, L);
+    const int kz = min(kz0 + (int)threadIdx.y, nzh - 1);
+    if (nout == 3) {
+        for (int k = threadIdx.x; k < m; k += blockDim.x) X[threadIdx.y * ld + k] = line[k];
+        __syncthreads();
+    }
+    auto output = [&](const float* __restrict__ tab, float2* out) {
+        const float2* src = (nout == 3) ? X + threadIdx.y * ld : line;
+        const float* tk = tab + (size_t)kz * m;
+        for (int k = threadIdx.x; k < m; k += blockDim.x) line[k] = cscale(src[k], __ldg(&tk[k]));
+        __syncthreads();
+        fft_m<+1>(smem, ld, fc, L);
+        for (int g = t0; g < tot; g += nthr) {
+            const int c = g & (L - 1), ix = g >> lg;
+            if (kz0 + c < nzh) out[(size_t)ix * nzh + kz0 + c] = smem[c * ld + ix];
+        }
+        __syncthreads();
+    };
+    output(a.tab0, a.out0);
+    if (nout == 3) {
+        output(a.tab1, a.out1);
+        output(a.tab2, a.out2);
+    }
+}
+
+// One-time construction of the per-kz convolution multipliers (see VtabArgs).
+__global__ void __launch_bounds__(768, 1) vz_convtab_kernel(VtabArgs a) {
+    extern __shared__ float2 smem[];
+    __shared__ FFTPass s_pass[QP_MAXST];
+    __shared__ FFTPass s_pass_c[QP_MAXST];
+    const FFTCtx fe = make_ctx(a.pl, s_pass);
+    const FFTCtx fcc = make_ctx(a.plc, s_pass_c);
+    const int L = a.L, n = a.nxx, m = a.plc.m, ld = max(a.pl.m, a.plc.m);
+    const int kz = blockIdx.x * L + threadIdx.y;
+    const bool valid = kz < a.nzh;
+    float2* line = smem + threadIdx.y * ld;
+    const double kzsq = a.kz2[valid ? kz : 0];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const double k2 = (double)a.kx2[k] + kzsq;
+        double s;
+        if (a.sym == 1) s = k2;
+        else if (a.sym == 0) s = pow(k2, 1.0 / 32.0);
+        else if (a.sym == 2) s = pow(k2, 33.0 / 32.0);
+        else s = pow(k2, 0.505);
+        line[k] = make_float2((float)s, 0.f);
+    }
+    __syncthreads();
+    dft_n<+1>(smem, ld, fe, L);  // sum_k s e^{+2 pi i k d/n}
+    // wrap to length m: lags 0..n-1 stay, lags -(n-1)..-1 go to m-n+1..m-1 (m >= 2n-1)
+    if (m > n) {
+        for (int dd = 1 + threadIdx.x; dd < n; dd += blockDim.x) line[m - dd] = line[n - dd];
+        __syncthreads();
+        for (int k = n + threadIdx.x; k <= m - n; k += blockDim.x) line[k] = make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < m; k += blockDim.x) line[k] = make_float2(line[k].x * a.norm, 0.f);
+    __syncthreads();
+    fft_m<-1>(smem, ld, fcc, L);
+    if (valid)
+        for (int k = threadIdx.x; k < m; k += blockDim.x) a.out[(size_t)kz * m + k] = line[k].x / (float)m;
+}
+
 // ---- z pass B -----------------------------------------------------------------
 __global__ void __launch_bounds__(768, 1) vz_passB_kernel(VzArgsB a) {
     ZPASS_SETUP
@@ -308,6 +394,12 @@ void launch_vz_passA(const VzArgsA& a, cudaStream_t s) {
 void launch_vz_xspec(const VxsArgs& a, cudaStream_t s) {
     vz_xspec_kernel<<<(a.nzh + a.L - 1) / a.L, dim3(a.pl.tx, a.L), lsm(a.L, a.pl.m, a.mode == 0 ? 2 : 1), s>>>(a);
 }
+void launch_vz_xspec_conv(const VxsArgs& a, cudaStream_t s) {
+    vz_xspec_conv_kernel<<<(a.nzh + a.L - 1) / a.L, dim3(a.plc.tx, a.L), lsm(a.L, a.plc.m, a.mode == 0 ? 2 : 1), s>>>(a);
+}
+void launch_vz_convtab(const VtabArgs& a, cudaStream_t s) {
+    vz_convtab_kernel<<<(a.nzh + a.L - 1) / a.L, dim3(max(a.pl.tx, a.plc.tx), a.L), lsm(a.L, max(a.pl.m, a.plc.m), 1), s>>>(a);
+}
 void launch_vz_passB(const VzArgsB& a, cudaStream_t s) {
     vz_passB_kernel<<<zgrid(a.nxx, a.L), dim3(a.pl.tx, a.L), lsm(a.L, a.pl.m, 2), s>>>(a);
 }
@@ -322,6 +414,8 @@ int vz_set_smem_limits() {
     int bad = 0;
     bad |= cudaFuncSetAttribute(vz_passA_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_xspec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_convtab_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_passB_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_passC_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_zinv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;

@@ -18,7 +18,7 @@ def _lib():
     qpstd.lib()
 
 
-@pytest.mark.parametrize("nx,nz", [(60, 40), (57, 33), (90, 51)])
+@pytest.mark.parametrize("nx,nz", [(60, 40), (57, 33), (90, 51), (83, 37)])  # 83+20 = 103: prime width
 def test_vaps_steps_from_random_state(nx, nz):
     d = small_shot(qpstd.VAPS, nx=nx, nz=nz, nt=8)
     rng = np.random.default_rng(nx + nz)
@@ -64,6 +64,17 @@ def test_qrtm_stabilised_filter_regime():
     """Large eta so the stabilised symbol departs from k^1.01 within the run."""
     d = small_shot(qpstd.QRTM, nt=200, snaps=5)
     d = dict(d, etas=1e4, etar=1e4)
+    obs = O.OracleShot(dict(d, kind=O.VAPS)).model()
+    ref_img, ref_ssg, _ = O.OracleShot(d).rtm(obs)
+    img, ssg = qpstd.rtm_shot(d, obs)
+    assert rel_l2(ssg, ref_ssg) < TOL
+    assert rel_l2(img, ref_img) < TOL
+
+
+def test_qrtm_prime_width_image():
+    """Padded width 103 (prime): exact x transforms need Bluestein, so the
+    stationary symbols run as per-kz convolutions on the smooth length."""
+    d = small_shot(qpstd.QRTM, nx=83, nt=200, snaps=6)
     obs = O.OracleShot(dict(d, kind=O.VAPS)).model()
     ref_img, ref_ssg, _ = O.OracleShot(d).rtm(obs)
     img, ssg = qpstd.rtm_shot(d, obs)
