@@ -258,6 +258,8 @@ def main():
     ap.add_argument("--e2e-shots", type=int, default=8)
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--shots", type=int, default=0,
+                    help="run only the first N shots of the workload (small cases for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_init()
@@ -272,6 +274,9 @@ def main():
     torch.cuda.set_device(local)
     qpstd.lib()
     shots, kname, seed, desc, obs_maker = workload(args.workload)
+    if 0 < args.shots < len(shots):
+        shots = shots[:args.shots]
+        desc = dict(desc, shots=len(shots), subset=f"first {len(shots)} shots of the workload")
     pts = sum(d["nxx"] * d["nzz"] for d in shots)
     B = qpstd.Batch(shots)
     streams = [torch.cuda.ExternalStream(p) for p in B.stream_ptrs()]

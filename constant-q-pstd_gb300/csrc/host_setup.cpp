@@ -312,4 +312,46 @@ void conv_table(const HostPlan& hp, const std::vector<std::complex<double>>& Hn,
     for (int k = 0; k < m; k++) out[k] = hm[k] / (double)m;
 }
 
+int fill_plan_dev(const HostPlan& hp, FFTPlanDev& d) {
+    d.n = hp.n;
+    d.m = hp.m;
+    d.blue = hp.blue;
+    d.nst = (int)hp.rad.size();
+    int ns = 1, maxb = 1;
+    for (int i = 0; i < d.nst; i++) {
+        FFTPass& p = d.pass[i];
+        p.R = hp.rad[i];
+        p.ns = ns;
+        p.B = hp.m / p.R;
+        p.twstride = hp.m / (ns * p.R);
+        p.ns_magic = (ns > 1) ? (unsigned)(((1ull << 32) + ns - 1) / ns) : 0u;
+        maxb = std::max(maxb, p.B);
+        ns *= p.R;
+    }
+    d.tx = std::min(QP_MAXTHREADS, (maxb + 31) / 32 * 32);
+    d.w = d.chirp = d.bhat = nullptr;
+    return (maxb > QP_MAXTHREADS) ? -1 : 0;
+}
+
+void plan_tables(const HostPlan& hp, std::vector<float2>& out) {
+    out.clear();
+    out.reserve(hp.w.size() + hp.chirp.size() + hp.bhat.size());
+    for (auto& c : hp.w) out.push_back(make_float2((float)c.real(), (float)c.imag()));
+    for (auto& c : hp.chirp) out.push_back(make_float2((float)c.real(), (float)c.imag()));
+    for (auto& c : hp.bhat) out.push_back(make_float2((float)c.real(), (float)c.imag()));
+}
+
+int choose_L(int nlines, int m, int tx, int nbuf, bool pow2, size_t extra_per_line, size_t budget) {
+    const size_t per_line = (size_t)8 * m * nbuf + extra_per_line;
+    const int lmax = std::max(1, std::min(QP_MAXTHREADS / tx, (int)(budget / per_line)));
+    int L = (nlines + 2 * 152 - 1) / (2 * 152);
+    L = std::max(1, std::min(L, lmax));
+    if (pow2) {
+        int p = 1;
+        while (p * 2 <= L) p *= 2;
+        L = p;
+    }
+    return L;
+}
+
 }  // namespace qp

@@ -32,4 +32,16 @@ int build_conv_plan_host(int n, HostPlan& hp);
 void conv_table(const HostPlan& hp, const std::vector<std::complex<double>>& Hn,
                 std::vector<std::complex<double>>& out);
 
+// Device view of a plan without its tables: passes, thread count per line.
+// Returns -1 when a pass needs more threads per line than a CTA holds.
+int fill_plan_dev(const HostPlan& hp, FFTPlanDev& d);
+// The plan's tables in device order: twiddles, then (Bluestein) chirp and bhat.
+void plan_tables(const HostPlan& hp, std::vector<float2>& out);
+
+// Complex lines per CTA: bounded by the CTA's threads (tx per line), by shared
+// memory (nbuf line buffers of m float2, plus extra_per_line bytes), and small
+// enough that the grid covers the 152 SMs about twice.  pow2: a power of two.
+int choose_L(int nlines, int m, int tx, int nbuf, bool pow2, size_t extra_per_line = 0,
+             size_t budget = 160 * 1024);
+
 }  // namespace qp

@@ -37,6 +37,31 @@ __device__ __forceinline__ void zload_pair(const float* __restrict__ f, float2* 
     }
 }
 
+// Half spectra in kz: S[ix*nzh + kz], kz in [0, nzz/2].  Two real z-lines a, b
+// share one complex line z = a + ib: A(k) = (Z(k) + conj Z(n-k))/2,
+// B(k) = (Z(k) - conj Z(n-k))/(2i), and back Z(k) = A(k) + iB(k).
+// this thread's packed line <- half spectra of rows (xa, xa+1)
+__device__ __forceinline__ void zrepack(const float2* __restrict__ S, float2* line, int nzz, int nzh, bool has0,
+                                        bool has1, int xa) {
+    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+        const int kk = (k < nzh) ? k : nzz - k;
+        const float2 A = has0 ? S[(size_t)xa * nzh + kk] : make_float2(0.f, 0.f);
+        const float2 B = has1 ? S[(size_t)(xa + 1) * nzh + kk] : make_float2(0.f, 0.f);
+        line[k] = (k < nzh) ? make_float2(A.x - B.y, A.y + B.x) : make_float2(A.x + B.y, -A.y + B.x);
+    }
+}
+
+// half spectra of rows (xa, xa+1) <- this thread's transformed packed line
+__device__ __forceinline__ void zunpack(const float2* line, float2* __restrict__ S, int nzz, int nzh, bool has0,
+                                        bool has1, int xa) {
+    for (int k = threadIdx.x; k < nzh; k += blockDim.x) {
+        const float2 z = line[k];
+        const float2 w = line[(k == 0) ? 0 : nzz - k];
+        if (has0) S[(size_t)xa * nzh + k] = make_float2(0.5f * (z.x + w.x), 0.5f * (z.y - w.y));
+        if (has1) S[(size_t)(xa + 1) * nzh + k] = make_float2(0.5f * (z.y + w.y), -0.5f * (z.x - w.x));
+    }
+}
+
 // x passes: a CTA owns TZ = 2L consecutive z columns (TZ a power of two); line
 // l holds columns (iz0+2l, iz0+2l+1) in re/im, indexed by x.  Global accesses
 // walk (ix, c) with c fastest so each x row is read as one TZ-float segment.

@@ -62,29 +62,10 @@ extern "C" int qpstd_version(void) { return 100; }
 __global__ void add_point_kernel(float* p, float v) { p[0] += v; }
 
 static int upload_plan(qpstd_shot* s, const HostPlan& hp, FFTPlanDev& d) {
-    d.n = hp.n;
-    d.m = hp.m;
-    d.blue = hp.blue;
-    d.nst = (int)hp.rad.size();
-    int ns = 1, maxb = 1;
-    for (int i = 0; i < d.nst; i++) {
-        FFTPass& p = d.pass[i];
-        p.R = hp.rad[i];
-        p.ns = ns;
-        p.B = hp.m / p.R;
-        p.twstride = hp.m / (ns * p.R);
-        p.ns_magic = (ns > 1) ? (unsigned)(((1ull << 32) + ns - 1) / ns) : 0u;
-        maxb = std::max(maxb, p.B);
-        ns *= p.R;
-    }
-    d.tx = std::min(QP_MAXTHREADS, (maxb + 31) / 32 * 32);
-    if (maxb > QP_MAXTHREADS) return fail(QPSTD_ENOTSUP, "transform needs more threads per line than a CTA holds");
-    const size_t cnt = hp.w.size() + hp.chirp.size() + hp.bhat.size();
-    std::vector<float2> h(cnt);
-    size_t o = 0;
-    for (auto& c : hp.w) h[o++] = make_float2((float)c.real(), (float)c.imag());
-    for (auto& c : hp.chirp) h[o++] = make_float2((float)c.real(), (float)c.imag());
-    for (auto& c : hp.bhat) h[o++] = make_float2((float)c.real(), (float)c.imag());
+    if (fill_plan_dev(hp, d)) return fail(QPSTD_ENOTSUP, "transform needs more threads per line than a CTA holds");
+    std::vector<float2> h;
+    plan_tables(hp, h);
+    const size_t cnt = h.size();
     float2* dptr = nullptr;
     CK(cudaMalloc(&dptr, sizeof(float2) * cnt));
     s->allocs.push_back(dptr);
@@ -93,23 +74,6 @@ static int upload_plan(qpstd_shot* s, const HostPlan& hp, FFTPlanDev& d) {
     d.chirp = hp.blue ? dptr + hp.w.size() : nullptr;
     d.bhat = hp.blue ? dptr + hp.w.size() + hp.chirp.size() : nullptr;
     return QPSTD_OK;
-}
-
-// Complex lines per CTA: bounded by the CTA's threads (tx per line), by shared
-// memory (nbuf line buffers of m float2), and small enough that the grid
-// covers the 152 SMs about twice.  pow2: x tiles need a power of two.
-static int choose_L(int nlines, int m, int tx, int nbuf, bool pow2, size_t extra_per_line = 0,
-                    size_t budget = 160 * 1024) {
-    const size_t per_line = (size_t)8 * m * nbuf + extra_per_line;
-    const int lmax = std::max(1, std::min(QP_MAXTHREADS / tx, (int)(budget / per_line)));
-    int L = (nlines + 2 * 152 - 1) / (2 * 152);
-    L = std::max(1, std::min(L, lmax));
-    if (pow2) {
-        int p = 1;
-        while (p * 2 <= L) p *= 2;
-        L = p;
-    }
-    return L;
 }
 
 static int validate(const qpstd_shot_desc* d) {

@@ -22,28 +22,6 @@
 
 namespace qp {
 
-// this thread's packed line <- half spectra of rows (xa, xa+1)
-__device__ __forceinline__ void zrepack(const float2* __restrict__ S, float2* line, int nzz, int nzh, bool has0,
-                                        bool has1, int xa) {
-    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
-        const int kk = (k < nzh) ? k : nzz - k;
-        const float2 A = has0 ? S[(size_t)xa * nzh + kk] : make_float2(0.f, 0.f);
-        const float2 B = has1 ? S[(size_t)(xa + 1) * nzh + kk] : make_float2(0.f, 0.f);
-        line[k] = (k < nzh) ? make_float2(A.x - B.y, A.y + B.x) : make_float2(A.x + B.y, -A.y + B.x);
-    }
-}
-
-// half spectra of rows (xa, xa+1) <- this thread's transformed packed line
-__device__ __forceinline__ void zunpack(const float2* line, float2* __restrict__ S, int nzz, int nzh, bool has0,
-                                        bool has1, int xa) {
-    for (int k = threadIdx.x; k < nzh; k += blockDim.x) {
-        const float2 z = line[k];
-        const float2 w = line[(k == 0) ? 0 : nzz - k];
-        if (has0) S[(size_t)xa * nzh + k] = make_float2(0.5f * (z.x + w.x), 0.5f * (z.y - w.y));
-        if (has1) S[(size_t)(xa + 1) * nzh + k] = make_float2(0.5f * (z.y + w.y), -0.5f * (z.x - w.x));
-    }
-}
-
 #define ZPASS_SETUP                                                  \
     extern __shared__ float2 smem[];                                 \
     __shared__ FFTPass s_pass[QP_MAXST];                             \

@@ -20,6 +20,7 @@ FUSED, PLAIN = 0, 1
 
 _fp = C.POINTER(C.c_float)
 _ip = C.POINTER(C.c_int)
+_dp = C.POINTER(C.c_double)
 
 
 class ShotDesc(C.Structure):
@@ -86,6 +87,14 @@ EXPORTS = {
     "qpstd_rtm_batch": (C.c_int, [C.POINTER(ShotDesc), C.c_int, C.POINTER(_fp), C.POINTER(_fp), C.POINTER(_fp)]),
     "qpstd_ac_advance_noalloc": (C.c_int, [C.POINTER(ShotDesc)] + [C.c_void_p] * 5
                                  + [C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
+    "qpstd_lowrank_decompose": (C.c_int, [C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, _fp, _fp, _fp,
+                                          C.c_int, C.c_int, C.c_ulonglong, _fp, _fp, _dp, _ip, _ip]),
+    "qpstd_lowrank_check": (C.c_int, [C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int,
+                                      _fp, _dp, _fp, _fp, _fp, _fp, C.c_int, _fp, _fp]),
+    "qpstd_lowrank_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _fp, _fp, _dp, C.POINTER(C.c_void_p)]),
+    "qpstd_lowrank_destroy": (C.c_int, [C.c_void_p]),
+    "qpstd_lowrank_apply": (C.c_int, [C.c_void_p, _fp, _fp]),
+    "qpstd_lowrank_apply_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 KIND_NAMES = ["xpass", "zpass", "xspec", "other", "plain"]
 
@@ -323,3 +332,58 @@ def rtm_batch(dicts, obs_list, method: int = FUSED):
     _check(lib().qpstd_rtm_batch(arr, len(dicts), po, pi, ps))
     return imgs, ssgs
 
+
+
+# ---- low-rank form of the constant-Q symbol ----------------------------------------
+def lowrank_decompose(nxx, nzz, dx, dz, dt, vp, tao, gam, row, col, seed=1):
+    """FP64 host decomposition (no GPU): dict with U (N1 x col), V (row x N2),
+    A (col x row, float64), jrr, irr."""
+    nxh, nzh = nxx // 2 + 1, nzz // 2 + 1
+    vp, tao, gam = (np.ascontiguousarray(a, dtype=np.float32).ravel() for a in (vp, tao, gam))
+    U = np.zeros((nxx * nzz, col), dtype=np.float32)
+    V = np.zeros((row, nxh * nzh), dtype=np.float32)
+    A = np.zeros((col, row), dtype=np.float64)
+    jrr = np.zeros(col, dtype=np.int32)
+    irr = np.zeros(row, dtype=np.int32)
+    _check(lib().qpstd_lowrank_decompose(nxx, nzz, dx, dz, dt, _f(vp), _f(tao), _f(gam), row, col, seed,
+                                         _f(U), _f(V), A.ctypes.data_as(_dp), jrr.ctypes.data_as(_ip),
+                                         irr.ctypes.data_as(_ip)))
+    return {"U": U, "V": V, "A": A, "jrr": jrr, "irr": irr, "nxx": nxx, "nzz": nzz, "row": row, "col": col}
+
+
+def lowrank_check(f, dx, dz, dt, vp, tao, gam, point):
+    """Exact and approximated rows W(x_point, k) on the half grid (host only)."""
+    n2 = f["V"].shape[1]
+    We, Wa = np.zeros(n2, dtype=np.float32), np.zeros(n2, dtype=np.float32)
+    vp, tao, gam = (np.ascontiguousarray(a, dtype=np.float32).ravel() for a in (vp, tao, gam))
+    _check(lib().qpstd_lowrank_check(f["nxx"], f["nzz"], dx, dz, dt, f["row"], f["col"], _f(f["U"]),
+                                     f["A"].ctypes.data_as(_dp), _f(f["V"]), _f(vp), _f(tao), _f(gam), point,
+                                     _f(We), _f(Wa)))
+    return We, Wa
+
+
+class LowRank:
+    """Device operator out = sum_a U[x,a] sum_b A[a,b] Re F^-1[Vt_b F in] / N."""
+
+    def __init__(self, f: dict):
+        self.f = f
+        self.h = C.c_void_p()
+        _check(lib().qpstd_lowrank_create(f["nxx"], f["nzz"], f["row"], f["col"], _f(f["U"]), _f(f["V"]),
+                                          f["A"].ctypes.data_as(_dp), C.byref(self.h)))
+
+    def apply(self, field: np.ndarray) -> np.ndarray:
+        a = np.ascontiguousarray(field, dtype=np.float32)
+        out = np.zeros_like(a)
+        _check(lib().qpstd_lowrank_apply(self.h, _f(a), _f(out)))
+        return out
+
+    def close(self):
+        if self.h:
+            lib().qpstd_lowrank_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -156,6 +156,36 @@ int qpstd_batch_pipeline_end(qpstd_batch *b);
 int qpstd_rtm_batch(const qpstd_shot_desc *d, int nshots, const float *const *obs, float *const *img,
                     float *const *ssg);
 
+/* ---- low-rank form of the constant-Q mixed-domain symbol -----------------
+ * W(x,k) = sinc(vp dt k^(1+gam)/2) k^gam sqrt(1 + dt tau k^1.01/2), sinc(u) =
+ * sin(u)/u, |k| on the half grid nxh x nzh (nxh = nxx/2+1, nzh = nzz/2+1,
+ * k[0] = 1e-6, cal_k2dh, sgpstd-qmodeling/func.c:783).  Replaces acsglowrank2d
+ * (sgpstd-qmodeling/sglowrank.c:148), whose call site is commented out in the
+ * reference (sgpstd-qmodeling/acsglw.cu:367-389).  FP64 setup, seeded (the
+ * reference seeds rand() from the clock).  Host only, no GPU needed.
+ * vp, tao, gam: nxx*nzz.  Outputs (each may be NULL): U nxx*nzz x col,
+ * V row x nxh*nzh, A col x row (double), jrr[col] chosen wavenumbers,
+ * irr[row] chosen points. */
+int qpstd_lowrank_decompose(int nxx, int nzz, float dx, float dz, float dt, const float *vp, const float *tao,
+                            const float *gam, int row, int col, unsigned long long seed, float *U, float *V,
+                            double *A, int *jrr, int *irr);
+/* Exact row W(x_is, k) and its low-rank approximation, nxh*nzh floats each
+ * (checka_error, sgpstd-qmodeling/sglowrank.c:61-101).  Host only. */
+int qpstd_lowrank_check(int nxx, int nzz, float dx, float dz, float dt, int row, int col, const float *U,
+                        const double *A, const float *V, const float *vp, const float *tao, const float *gam,
+                        int is, float *We, float *Wa);
+/* Device operator out = sum_a U[x][a] sum_b A[a][b] Re F^-1[Vt_b F in](x) / N
+ * (the reference's multv_kernel / sumlw_kernel / sumlw2_kernel,
+ * sgpstd-qmodeling/acsglw.cu:1375-1497, with Vt_b = consist_Vt of V_b). */
+typedef struct qpstd_lowrank qpstd_lowrank;
+int qpstd_lowrank_create(int nxx, int nzz, int row, int col, const float *U, const float *V, const double *A,
+                         qpstd_lowrank **out);
+int qpstd_lowrank_destroy(qpstd_lowrank *h);
+/* in, out: host nxx*nzz. */
+int qpstd_lowrank_apply(qpstd_lowrank *h, const float *in, float *out);
+/* d_in, d_out: device nxx*nzz; stream: cudaStream_t (NULL: the handle's own). No sync. */
+int qpstd_lowrank_apply_device(qpstd_lowrank *h, const float *d_in, float *d_out, void *stream);
+
 /* ---- acoustic steps without device allocation ---------------------------
  * No counterpart in the reference (its acforward allocates all device memory
  * itself).  For callers that cannot call cudaMalloc -- code running while

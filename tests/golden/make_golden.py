@@ -52,6 +52,7 @@ def main():
     qm_a.get_pml_parameters.argtypes = [C.c_int, C.c_float] + [fp] * 8 + [C.c_int, C.c_int, C.c_float, C.c_float, C.c_float]
     qm_a.cal_shift_parameters.argtypes = [fp] * 8 + [C.c_float, C.c_float, C.c_int, C.c_int]
     qm_f.cal_k2d.argtypes = [C.c_float, C.c_float, C.c_int, C.c_int] + [fp] * 4
+    qm_f.cal_k2dh.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, fp]
     qm_a.rik_cal.argtypes = [C.c_int, C.c_float, C.c_float, fp, C.c_int]
     qm_a.cal_bbx_bbz.argtypes = [C.c_int, C.c_int, fp, fp, fp]
     qm_f.transfermodel.argtypes = [C.c_int, C.c_int, C.c_float, C.c_float] + [fp] * 6
@@ -74,6 +75,11 @@ def main():
             qm_f.cal_k2d(dx, dz, nxx, nzz, *[pf(a) for a in ks])
             for k, a in zip(["k2d1", "k2d2", "k2d3", "k2da"], ks):
                 out[f"g{g}_{k}"] = a
+            # |k| on the half grid, the wavenumbers of the low-rank form
+            nxh, nzh = nxx // 2 + 1, nzz // 2 + 1
+            kh = f32(nxh * nzh)
+            qm_f.cal_k2dh(nxh, nzh, nxx, nzz, dx, dz, pf(kh))
+            out[f"g{g}_k2dh"] = kh
         out[f"g{g}_grid"] = np.array([pml, fd, nxx, nzz, dx, dz, dt], dtype=np.float64)
     for flag in (1, 2):
         r = f32(3000)
