@@ -247,6 +247,105 @@ def run_reference(args, ws, rank):
     print(json.dumps(out), flush=True)
 
 
+def serve_requests(n: int, seed: int, nt_scale: float):
+    """Config 5 request stream: kinds 40/30/20/10 % aps/vaps/artm/qrtm, model
+    grids log-uniform from 256 x 256 to 2048 (z) x 4096 (x), nt ~ U(2000, 8000)
+    (times nt_scale), CPML 20, dx = dz = 10 m, dt = 0.5 ms, 30 snapshots."""
+    import qpstd
+    rng = np.random.default_rng(seed)
+    kinds = rng.choice([qpstd.APS, qpstd.VAPS, qpstd.ARTM, qpstd.QRTM], size=n, p=[0.4, 0.3, 0.2, 0.1])
+    nz = np.exp(rng.uniform(np.log(256), np.log(2048), n)).astype(int)
+    nx = np.exp(rng.uniform(np.log(256), np.log(4096), n)).astype(int)
+    nt = np.maximum(50, (rng.integers(2000, 8001, n) * nt_scale).astype(int))
+    return [(int(k), int(x), int(z), int(t), seed * 1000 + i) for i, (k, x, z, t) in enumerate(zip(kinds, nx, nz, nt))]
+
+
+def run_serve(args, ws, rank):
+    """Serving mix (config 5) through qpstd_server: Poisson arrivals, latency
+    p50/p99, shots/hour; the plain per-shot path serves the same stream one
+    request at a time (FIFO from the measured plain service times)."""
+    import torch
+
+    import qpstd
+    import workloads as W
+
+    seed = 1005
+    reqs = serve_requests(args.requests, seed, args.nt_scale)
+    shots, obs = [], []
+    for (k, nx, nz, nt, s) in reqs:
+        d = W.make_shot(k, nx, nz, 20, nt, 0.0005, 20.0, s, nlayers=6, nanom=1, snaps=30)
+        shots.append(d)
+        obs.append(synthetic_obs(d, s) if k in (qpstd.ARTM, qpstd.QRTM) else None)
+    pts = np.array([d["nxx"] * d["nzz"] for d in shots], dtype=np.float64)
+    cnt = np.array([d["nt"] * (2 if d["kind"] in (qpstd.ARTM, qpstd.QRTM) else 1) for d in shots], dtype=np.float64)
+    work = float((pts * cnt).sum())
+    # arrival rate: the stream offers `load` times the work a 3 Gpts/s server finishes
+    rng = np.random.default_rng(seed + 1)
+    span = work / 3.0e9 / args.load
+    gaps = rng.exponential(span / len(shots), size=len(shots))
+    arrive = np.cumsum(gaps) - gaps[0]
+    torch.cuda.set_device(0)
+    qpstd.lib()
+    sv = qpstd.Server(mem_budget=0, max_active=64)
+    t0 = time.perf_counter()
+    ids = []
+    for i, d in enumerate(shots):
+        wait = arrive[i] - (time.perf_counter() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        ids.append(sv.submit(d, obs[i]))
+    sv.wait()
+    wall = time.perf_counter() - t0
+    lat, snaps = [], []
+    for rid in ids:
+        st, l, sn = sv.status(rid)
+        if st != 2:
+            raise SystemExit(f"request {rid} failed with status {st}")
+        lat.append(l)
+        snaps.append(sn)
+    sv.close()
+    lat = np.array(lat)
+    # plain path: each request alone, served FIFO in arrival order
+    serv = []
+    for d, o in zip(shots, obs):
+        a = time.perf_counter()
+        if o is None:
+            qpstd.model_shot(d, method=qpstd.PLAIN)
+        else:
+            qpstd.rtm_shot(d, o, method=qpstd.PLAIN)
+        serv.append(time.perf_counter() - a)
+    fin, plat = 0.0, []
+    for a, s in zip(arrive, serv):
+        fin = max(fin, a) + s
+        plat.append(fin - a)
+    plat = np.array(plat)
+    pwall = fin
+    h2d = int(sum(4 * (12 * d["nxx"] * d["nzz"] + d["nt"]) + (4 * o.size if o is not None else 0)
+                  for d, o in zip(shots, obs)))
+    d2h = int(sum(4 * (d["nt"] * len(d["gxg"]) if o is None else 2 * (d["nxx"] - 40) * (d["nzz"] - 40))
+                  for d, o in zip(shots, obs)))
+    val = work / wall / 1e9
+    out = {
+        "metric": METRIC, "value": val, "unit": "Gpts/s", "n_gpus": 1, "steps": len(shots), "warmup": 0,
+        "ms_per_step": 1000.0 * wall / len(shots), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": f"synthetic (seeded request stream, seed {seed})",
+        "config": {"workload": "serve5", "requests": len(shots), "mix": "40/30/20/10 % aps/vaps/artm/qrtm",
+                   "grids": "log-uniform 256x256 .. 2048x4096, CPML 20", "nt_scale": args.nt_scale,
+                   "arrivals": f"Poisson, offered load {args.load} x a 3 Gpts/s server",
+                   "step": "one request (value = grid-point updates / wall from first arrival to last result)"},
+        "serving": {"wall_s": wall, "shots_per_hour": 3600.0 * len(shots) / wall,
+                    "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                    "snaps_used_min": int(min(s for s in snaps if s > 0)) if any(snaps) else None,
+                    "plain_per_shot": {"wall_s": pwall, "shots_per_hour": 3600.0 * len(shots) / pwall,
+                                       "p50_s": float(np.percentile(plat, 50)),
+                                       "p99_s": float(np.percentile(plat, 99)),
+                                       "gpts_per_s": work / pwall / 1e9}},
+        "e2e": {"value": val, "unit": "Gpts/s", "h2d_bytes_per_step": h2d // len(shots),
+                "d2h_bytes_per_step": d2h // len(shots)},
+    }
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -260,11 +359,18 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--shots", type=int, default=0,
                     help="run only the first N shots of the workload (small cases for profiling)")
+    ap.add_argument("--requests", type=int, default=500, help="serve5: requests in the stream")
+    ap.add_argument("--nt-scale", type=float, default=1.0, help="serve5: scale of the nt draws")
+    ap.add_argument("--load", type=float, default=1.0, help="serve5: offered load (x a 3 Gpts/s server)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_init()
     if args.impl == "reference":
         run_reference(args, ws, rank)
+        return
+    if args.workload == "serve5":
+        if rank == 0:
+            run_serve(args, ws, rank)
         return
 
     import torch

@@ -165,30 +165,46 @@ inline unsigned nblk(size_t n) { return (unsigned)((n + TB - 1) / TB); }
 
 }  // namespace
 
+// The 2-D C2C plan of the window (cufftPlan2d in the reference,
+// sgpstd-qmodeling/acps4.cu:871-872) with its work area and the five complex
+// scratch fields taken from the shot's own buffers (so a server's arena holds
+// them too).
 int plain_setup(qpstd_shot* s, std::string& err) {
     PlainState& P = s->plain;
     const size_t N = s->N;
-    if (cufftPlan2d(&P.plan, s->d.nxx, s->d.nzz, CUFFT_C2C) != CUFFT_SUCCESS) {
-        err = "cufftPlan2d failed";
+    size_t ws = 0;
+    if (cufftCreate(&P.plan) != CUFFT_SUCCESS) {
+        err = "cufftCreate failed";
         return -1;
     }
     P.have_plan = true;
-    if (cufftSetStream(P.plan, s->stream) != CUFFT_SUCCESS) {
-        err = "cufftSetStream failed";
+    if (cufftSetAutoAllocation(P.plan, 0) != CUFFT_SUCCESS ||
+        cufftMakePlan2d(P.plan, s->d.nxx, s->d.nzz, CUFFT_C2C, &ws) != CUFFT_SUCCESS) {
+        err = "cufftMakePlan2d failed";
         return -1;
     }
-    if (cudaMalloc(&P.dis, sizeof(float2) * 5 * N) != cudaSuccess) {
-        err = "cudaMalloc of the plain scratch failed";
+    void* work = nullptr;
+    if (ws > 0 && shot_malloc(s, &work, ws) != cudaSuccess) {
+        err = "no device memory for the cuFFT work area";
+        return -1;
+    }
+    if ((ws > 0 && cufftSetWorkArea(P.plan, work) != CUFFT_SUCCESS) ||
+        cufftSetStream(P.plan, s->stream) != CUFFT_SUCCESS) {
+        err = "cufftSetWorkArea / cufftSetStream failed";
+        return -1;
+    }
+    if (shot_malloc(s, (void**)&P.dis, sizeof(float2) * 5 * N) != cudaSuccess) {
+        err = "no device memory for the plain scratch";
         return -1;
     }
     return 0;
 }
 
+// The plan only: the buffers are the shot's and go with them.
 void plain_release(qpstd_shot* s) {
     PlainState& P = s->plain;
     if (P.have_plan) cufftDestroy(P.plan);
     P.have_plan = false;
-    if (P.dis) cudaFree(P.dis);
     P.dis = nullptr;
 }
 

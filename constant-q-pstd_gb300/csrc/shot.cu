@@ -10,7 +10,10 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -61,14 +64,27 @@ extern "C" int qpstd_version(void) { return 100; }
 // ---------------------------------------------------------------------------
 __global__ void add_point_kernel(float* p, float v) { p[0] += v; }
 
+// Every device buffer of a shot: from its arena when it has one (shots of a
+// server), else cudaMalloc; recorded for release at destroy.
+cudaError_t shot_malloc(qpstd_shot* s, void** p, size_t bytes) {
+    if (s->arena) {
+        *p = s->arena->alloc(bytes);
+        if (!*p) return cudaErrorMemoryAllocation;
+    } else {
+        const cudaError_t e = cudaMalloc(p, bytes);
+        if (e != cudaSuccess) return e;
+    }
+    s->allocs.push_back(*p);
+    return cudaSuccess;
+}
+
 static int upload_plan(qpstd_shot* s, const HostPlan& hp, FFTPlanDev& d) {
     if (fill_plan_dev(hp, d)) return fail(QPSTD_ENOTSUP, "transform needs more threads per line than a CTA holds");
     std::vector<float2> h;
     plan_tables(hp, h);
     const size_t cnt = h.size();
     float2* dptr = nullptr;
-    CK(cudaMalloc(&dptr, sizeof(float2) * cnt));
-    s->allocs.push_back(dptr);
+    CK(shot_malloc(s, (void**)&dptr, sizeof(float2) * cnt));
     CK(cudaMemcpy(dptr, h.data(), sizeof(float2) * cnt, cudaMemcpyHostToDevice));
     d.w = dptr;
     d.chirp = hp.blue ? dptr + hp.w.size() : nullptr;
@@ -99,12 +115,11 @@ static int validate(const qpstd_shot_desc* d) {
 
 static float* dalloc(qpstd_shot* s, size_t n, int* rc) {
     float* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, sizeof(float) * n);
+    cudaError_t e = shot_malloc(s, (void**)&p, sizeof(float) * n);
     if (e != cudaSuccess) {
         *rc = cuda_fail(e, "cudaMalloc");
         return nullptr;
     }
-    s->allocs.push_back(p);
     return p;
 }
 
@@ -139,13 +154,11 @@ static int build_rec_list(qpstd_shot* s, const qpstd_shot_desc* d, int width, bo
     }
     off[ntile] = (int)flat.size();
     int* doff = nullptr;
-    CK(cudaMalloc(&doff, sizeof(int) * off.size()));
-    s->allocs.push_back(doff);
+    CK(shot_malloc(s, (void**)&doff, sizeof(int) * off.size()));
     CK(cudaMemcpy(doff, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
     RecEntry* drec = nullptr;
     const size_t nrec = std::max<size_t>(flat.size(), 1);
-    CK(cudaMalloc(&drec, sizeof(RecEntry) * nrec));
-    s->allocs.push_back(drec);
+    CK(shot_malloc(s, (void**)&drec, sizeof(RecEntry) * nrec));
     if (!flat.empty()) CK(cudaMemcpy(drec, flat.data(), sizeof(RecEntry) * flat.size(), cudaMemcpyHostToDevice));
     *off_out = doff;
     *rec_out = drec;
@@ -250,8 +263,7 @@ static int setup_plain(qpstd_shot* s, const qpstd_shot_desc* d) {
     const size_t nc = 2 * (size_t)d->nxx + 2 * d->nzz;
     std::vector<float2> hc(nc);
     float2* cbase = nullptr;
-    CK(cudaMalloc(&cbase, sizeof(float2) * nc));
-    s->allocs.push_back(cbase);
+    CK(shot_malloc(s, (void**)&cbase, sizeof(float2) * nc));
     const float2** dst[4] = {&s->plain.HxM, &s->plain.HxP, &s->plain.HzM, &s->plain.HzP};
     size_t q = 0;
     std::vector<std::complex<double>> H;
@@ -276,8 +288,7 @@ static int setup_conv(qpstd_shot* s, const qpstd_shot_desc* d) {
     const size_t nc = 3 * (size_t)cx.m + 3 * (size_t)cz.m;
     std::vector<float2> hc(nc);
     float2* base = nullptr;
-    CK(cudaMalloc(&base, sizeof(float2) * nc));
-    s->allocs.push_back(base);
+    CK(shot_malloc(s, (void**)&base, sizeof(float2) * nc));
     size_t q = 0;
     std::vector<std::complex<double>> H, T;
     auto put = [&](const HostPlan& hp, const std::vector<std::complex<double>>& sym, const float2** dst) {
@@ -309,13 +320,20 @@ static int setup_conv(qpstd_shot* s, const qpstd_shot_desc* d) {
     return QPSTD_OK;
 }
 
+static int autotune(qpstd_shot* s);
+
 extern "C" int qpstd_shot_create(const qpstd_shot_desc* d, qpstd_shot** out) {
+    return shot_create_ex(d, out, true, nullptr);
+}
+
+int shot_create_ex(const qpstd_shot_desc* d, qpstd_shot** out, bool tune, qp::Arena* arena) {
     if (!out) return fail(QPSTD_EINVAL, "null output handle");
     *out = nullptr;
     int rc = validate(d);
     if (rc) return rc;
     qpstd_shot* s = new qpstd_shot();
     s->d = *d;
+    s->arena = arena;
     const int nxx = d->nxx, nzz = d->nzz;
     const size_t N = (size_t)nxx * nzz;
     s->N = N;
@@ -392,8 +410,8 @@ extern "C" int qpstd_shot_create(const qpstd_shot_desc* d, qpstd_shot** out) {
         const size_t nc = 2 * (size_t)nxx + 2 * nzz;
         std::vector<float2> hc(nc);
         float2* cbase = nullptr;
-        if ((e = cudaMalloc(&cbase, sizeof(float2) * nc)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc"));
-        s->allocs.push_back(cbase);
+        if ((e = shot_malloc(s, (void**)&cbase, sizeof(float2) * nc)) != cudaSuccess)
+            return bail(cuda_fail(e, "cudaMalloc"));
         size_t q = 0;
         const float2** cdst[4] = {&s->HxM, &s->HxP, &s->HzM, &s->HzP};
         const int lens[4] = {nxx, nxx, nzz, nzz};
@@ -405,8 +423,8 @@ extern "C" int qpstd_shot_create(const qpstd_shot_desc* d, qpstd_shot** out) {
         }
         if ((e = cudaMemcpy(cbase, hc.data(), sizeof(float2) * nc, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(cuda_fail(e, "upload"));
     }
-    // FFT plans and tile shapes
-    {
+    // FFT plans and tile shapes of the fused passes (the plain form uses cuFFT)
+    if (d->method == QPSTD_FUSED) {
         HostPlan hx, hz;
         if (build_plan_host(nxx, hx) || build_plan_host(nzz, hz)) return bail(fail(QPSTD_ENOTSUP, "no FFT plan for this length"));
         if ((rc = upload_plan(s, hx, s->px))) return bail(rc);
@@ -432,9 +450,8 @@ extern "C" int qpstd_shot_create(const qpstd_shot_desc* d, qpstd_shot** out) {
     }
     if (s->visco && (rc = setup_visco(s, d))) return bail(rc);
     if ((rc = setup_ksq(s, d))) return bail(rc);
-    if (s->visco && (rc = setup_xtabs(s, d))) return bail(rc);
+    if (s->visco && d->method == QPSTD_FUSED && (rc = setup_xtabs(s, d))) return bail(rc);
     if (d->method == QPSTD_PLAIN && (rc = setup_plain(s, d))) return bail(rc);
-    if ((rc = build_receivers(s, d))) return bail(rc);
     s->gather = dalloc(s, (size_t)d->nt * std::max(d->nr, 1), &rc);
     if (!s->gather) return bail(rc);
     if (s->rtm) {
@@ -446,6 +463,11 @@ extern "C" int qpstd_shot_create(const qpstd_shot_desc* d, qpstd_shot** out) {
         s->ssg = s->img_c + (size_t)s->nx * s->nz;
         s->ssg_c = s->ssg + (size_t)s->nx * s->nz;
     }
+    // the receiver lists are grouped by the CTA tiles (x pass: 2*Lx z columns,
+    // z pass C: 2*Lzv x rows), so they are built once the tile sizes are final
+    if (tune && (rc = autotune(s))) return bail(rc);
+    if ((rc = build_receivers(s, d))) return bail(rc);
+    s->src.aux_pending = false;
     if ((e = cudaMemset(s->src.st, 0, sizeof(float) * 9 * N)) != cudaSuccess) return bail(cuda_fail(e, "memset"));
     *out = s;
     return QPSTD_OK;
@@ -460,7 +482,10 @@ extern "C" int qpstd_shot_destroy(qpstd_shot* s) {
     }
     for (cudaEvent_t e : s->evpool) cudaEventDestroy(e);
     plain_release(s);
-    for (void* p : s->allocs) cudaFree(p);
+    for (void* p : s->allocs) {
+        if (s->arena) s->arena->release(p);
+        else cudaFree(p);
+    }
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return QPSTD_OK;
@@ -730,8 +755,10 @@ static void src_step(qpstd_shot* s, int t, bool first, bool last, float* gather_
     x.xs = s->d.xsg;
     x.zs = s->d.zsg;
     x.src = src_amp(s, t);
-    x.rec_off = s->rec_off;
-    x.rec = s->rec;
+    if (gather_row) {
+        x.rec_off = s->rec_off;
+        x.rec = s->rec;
+    }
     x.gather_row = gather_row;
     if (ssg_on) {
         x.ssg = s->ssg;
@@ -751,6 +778,108 @@ static void src_end(qpstd_shot* s) {
     launch_ac_zpass(zargs(s, s->src, 1, 0), s->stream);
 }
 
+// ---- autotuning of the lines per CTA -------------------------------------------
+// Every pass kernel family runs L lines per CTA; L trades resident CTAs per SM
+// (latency hiding across barriers) against grid size, tail and shared memory.
+// At shot creation each family's admissible L (threads <= 768, shared memory
+// within the kernel's limit, powers of two where the tile needs it) are timed
+// in whole pipelined steps on the shot's own buffers -- zero state, no source
+// (t = -1), no recording, so every field stays zero -- one family after the
+// other, keeping the fastest.  Results are cached per grid shape for the
+// process.  QPSTD_AUTOTUNE=0 keeps the built-in choice.
+namespace {
+struct Knob {
+    int* L;
+    int lmax;
+    bool pow2;
+};
+std::mutex g_tune_mu;
+std::map<std::vector<int>, std::vector<int>> g_tune_cache;
+
+int lmax_of(int tx, size_t per_line, size_t budget) {
+    return std::max(1, std::min(QP_MAXTHREADS / std::max(tx, 1), (int)(budget / std::max<size_t>(per_line, 1))));
+}
+}  // namespace
+
+static float time_steps(qpstd_shot* s, int warm, int n) {
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    src_begin(s);
+    for (int i = 0; i < warm; i++) src_step(s, -1, i == 0, false, nullptr, false);
+    cudaEventRecord(a, s->stream);
+    for (int i = 0; i < n; i++) src_step(s, -1, false, i == n - 1, nullptr, false);
+    cudaEventRecord(b, s->stream);
+    src_end(s);
+    float ms = -1.f;
+    if (cudaEventSynchronize(b) == cudaSuccess) cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms;
+}
+
+static int autotune(qpstd_shot* s) {
+    const char* env = getenv("QPSTD_AUTOTUNE");
+    if (s->d.method != QPSTD_FUSED || (env && env[0] == '0')) return QPSTD_OK;
+    const size_t stz = (size_t)40 * s->d.nzz, stx = (size_t)72 * s->d.nxx;
+    std::vector<Knob> knobs;
+    if (s->visco) {
+        const int mz = std::max(s->pz.m, s->pzc.m), tz = std::max(s->pz.tx, s->pzc.tx);
+        const FFTPlanDev& pxs = s->xconv ? s->pxc : s->px;
+        knobs.push_back({&s->Lzv, lmax_of(tz, (size_t)16 * mz, 160 * 1024), false});
+        knobs.push_back({&s->Lxs3, lmax_of(pxs.tx, (size_t)16 * pxs.m, 160 * 1024), true});
+        knobs.push_back({&s->Lxs, lmax_of(pxs.tx, (size_t)8 * pxs.m, 160 * 1024), true});
+        if (s->xconv && s->d.kind == QPSTD_QRTM)
+            knobs.push_back({&s->Lxs_exact, lmax_of(s->px.tx, (size_t)8 * s->px.m, 160 * 1024), true});
+    } else {
+        knobs.push_back({&s->Lzp, lmax_of(s->pzc.tx, (size_t)8 * s->pzc.m + (s->stage_z ? stz : 0), QP_SMEM_DYN_MAX),
+                         false});
+    }
+    knobs.push_back({&s->Lx, lmax_of(s->pxc.tx, (size_t)8 * s->pxc.m + (s->stage_x ? stx : 0), QP_SMEM_DYN_MAX), true});
+    const std::vector<int> key = {s->d.kind, s->d.nxx, s->d.nzz};
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end() && it->second.size() == knobs.size()) {
+            for (size_t i = 0; i < knobs.size(); i++) *knobs[i].L = it->second[i];
+            return QPSTD_OK;
+        }
+    }
+    // scratch spectra hold whatever cudaMalloc left: clear them so the zero state stays zero
+    for (int k = 0; k < 4; k++)
+        if (s->spec[k]) cudaMemsetAsync(s->spec[k], 0, sizeof(float2) * (size_t)s->d.nxx * s->nzh, s->stream);
+    cudaMemsetAsync(s->src.st, 0, sizeof(float) * 9 * s->N, s->stream);
+    const bool prof = s->prof;
+    s->prof = false;
+    for (Knob& k : knobs) {
+        const int cur = *k.L;
+        std::vector<int> cand = {cur};
+        for (int L : {1, 2, 3, 4, 6, 8, 12, 16})
+            if (L <= k.lmax && L != cur && (!k.pow2 || (L & (L - 1)) == 0)) cand.push_back(L);
+        int best = cur;
+        float tbest = 1e30f;
+        for (int L : cand) {
+            *k.L = L;
+            float t = time_steps(s, 1, 3);
+            t = std::min(t, time_steps(s, 0, 3));
+            if (t > 0.f && t < tbest) {
+                tbest = t;
+                best = L;
+            }
+        }
+        *k.L = best;
+    }
+    s->prof = prof;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "autotune");
+    std::vector<int> val;
+    for (Knob& k : knobs) val.push_back(*k.L);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = val;
+    return QPSTD_OK;
+}
+
 // Advance the source wavefield over steps t0 .. t0+n-1 (source wavelet index t).
 // gather: device rows for each step (row t-t0), or null.
 static int advance_src(qpstd_shot* s, int t0, int n, float* gather, bool ssg_on) {
@@ -761,6 +890,56 @@ static int advance_src(qpstd_shot* s, int t0, int n, float* gather, bool ssg_on)
     src_end(s);
     if (s->plain_err) return fail(QPSTD_ECUDA, "plain step failed (cuFFT or launch)");
     cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    return QPSTD_OK;
+}
+
+// Device bytes qpstd_shot_create takes for d (the buffers above, each rounded
+// to 256 bytes, plus 1 MiB for the small tables); the plain form adds its
+// complex scratch and a cuFFT work area of the same order.
+extern "C" long long qpstd_shot_bytes(const qpstd_shot_desc* d) {
+    if (!d || d->nxx < 1 || d->nzz < 1 || d->nt < 1) return -1;
+    const bool visco = d->kind == QPSTD_VAPS || d->kind == QPSTD_QRTM;
+    const bool rtm = d->kind == QPSTD_ARTM || d->kind == QPSTD_QRTM;
+    const double N = (double)d->nxx * d->nzz, nzh = d->nzz / 2 + 1, NS = d->nxx * nzh;
+    const double nr = std::max(d->nr, 1), nx = d->nxx - 2 * d->pml, nz = d->nzz - 2 * d->pml;
+    const bool fused = d->method != QPSTD_PLAIN;
+    HostPlan cx, cz, ex, ez;
+    if (fused && (build_conv_plan_host(d->nxx, cx) || build_conv_plan_host(d->nzz, cz) ||
+                  build_plan_host(d->nxx, ex) || build_plan_host(d->nzz, ez)))
+        return -1;  // no fused plan for these lengths
+    double f = (rtm ? 18.0 : 9.0) * N + 6.0 * N;                       // wavefields; div, Lz, bbx, bbz, c1, c2
+    if (fused) {
+        f += 2.0 * (cx.m + cz.m) + 6.0 * (cx.m + cz.m);                // convolution plans and multipliers
+        f += 2.0 * (2.0 * ex.m + d->nxx) + 2.0 * (2.0 * ez.m + d->nzz);  // exact plans (twiddles, chirp, bhat)
+    }
+    f += 16.0 * (d->nxx + d->nzz);                                     // CPML profiles, squared wavenumbers
+    if (visco) {
+        f += 8.0 * N + 2.0 * NS * (rtm ? 6 : 5) + 4.0 * (d->nxx + d->nzz);
+        if (fused && ex.blue) f += 4.0 * nzh * cx.m;                   // per-kz convolution tables
+    }
+    f += (double)d->nt * nr;                                           // gather
+    if (rtm) f += (double)d->snaps * 8.0 * N + (double)d->nt * nr + 4.0 * nx * nz;
+    if (d->method == QPSTD_PLAIN) f += 20.0 * N;
+    return (long long)(4.0 * f) + 32 * 256 + (1ll << 20);
+}
+
+// Modeling in slices, for callers that interleave many shots: steps t0 .. t0+n-1
+// of the source wavefield with the gather rows recorded on the device (row t of
+// s->gather).  The slice at t0 = 0 starts the pipeline and the slice that
+// reaches nt completes it, so consecutive slices equal one advance over 0..nt-1.
+int model_slice(qpstd_shot* s, int t0, int n) {
+    if (!s || n <= 0 || t0 < 0 || t0 + n > s->d.nt) return fail(QPSTD_EINVAL, "bad modeling slice");
+    const int nt = s->d.nt, nr = s->d.nr;
+    if (t0 == 0) {
+        s->launches = 0;
+        src_begin(s);
+    }
+    for (int t = t0; t < t0 + n; t++)
+        src_step(s, t, t == 0, t == nt - 1, nr > 0 ? s->gather + (size_t)t * nr : nullptr, false);
+    if (t0 + n == nt) src_end(s);
+    if (s->plain_err) return fail(QPSTD_ECUDA, "plain step failed (cuFFT or launch)");
+    const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
     return QPSTD_OK;
 }

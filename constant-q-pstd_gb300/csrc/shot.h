@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "../../include/qpstd.h"
+#include "arena.h"
 #include "plain.h"
 #include "qpstd_internal.h"
 #include "revolve.h"
@@ -46,6 +47,13 @@ struct RtmRun {
 struct qpstd_shot;
 int rtm_begin(qpstd_shot* s);
 int rtm_action(qpstd_shot* s);  // 0: more actions, 1: finished, < 0: error code
+// qpstd_shot_create with options: tune runs the lines-per-CTA autotuner, arena
+// (may be null) supplies the device buffers.
+int shot_create_ex(const qpstd_shot_desc* d, qpstd_shot** out, bool tune, qp::Arena* arena);
+// Modeling steps t0 .. t0+n-1 with the gather kept on the device (see shot.cu).
+int model_slice(qpstd_shot* s, int t0, int n);
+// A device buffer owned by the shot (its arena's when it has one); freed at destroy.
+cudaError_t shot_malloc(qpstd_shot* s, void** p, size_t bytes);
 
 struct qpstd_shot {
     qp::RtmRun run;
@@ -55,6 +63,7 @@ struct qpstd_shot {
     bool visco = false, rtm = false;
     cudaStream_t stream = nullptr;
     std::vector<void*> allocs;
+    qp::Arena* arena = nullptr;  // device buffers come from here when set (server shots)
     qp::Wave src, rcv;
     float *div = nullptr, *Lz = nullptr;
     float *bbx = nullptr, *bbz = nullptr, *c1 = nullptr, *c2 = nullptr;

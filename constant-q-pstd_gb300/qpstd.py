@@ -95,6 +95,12 @@ EXPORTS = {
     "qpstd_lowrank_destroy": (C.c_int, [C.c_void_p]),
     "qpstd_lowrank_apply": (C.c_int, [C.c_void_p, _fp, _fp]),
     "qpstd_lowrank_apply_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "qpstd_shot_bytes": (C.c_longlong, [C.POINTER(ShotDesc)]),
+    "qpstd_server_create": (C.c_int, [C.c_longlong, C.c_int, C.POINTER(C.c_void_p)]),
+    "qpstd_server_destroy": (C.c_int, [C.c_void_p]),
+    "qpstd_server_submit": (C.c_longlong, [C.c_void_p, C.POINTER(ShotDesc), _fp, _fp, _fp]),
+    "qpstd_server_status": (C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+    "qpstd_server_wait": (C.c_int, [C.c_void_p, C.c_longlong]),
 }
 KIND_NAMES = ["xpass", "zpass", "xspec", "other", "plain"]
 
@@ -380,6 +386,64 @@ class LowRank:
     def close(self):
         if self.h:
             lib().qpstd_lowrank_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---- serving ----------------------------------------------------------------------
+def shot_bytes(d: dict) -> int:
+    D = Desc(d)
+    return int(lib().qpstd_shot_bytes(C.byref(D.s)))
+
+
+class Server:
+    """Continuous batching of shot requests (qpstd_server).  Keeps every
+    request's descriptor arrays and buffers alive until the request is done."""
+
+    def __init__(self, mem_budget: int = 0, max_active: int = 0):
+        self.h = C.c_void_p()
+        _check(lib().qpstd_server_create(int(mem_budget), int(max_active), C.byref(self.h)))
+        self.keep = {}
+
+    def submit(self, d: dict, obs: np.ndarray | None = None) -> int:
+        D = Desc(d)
+        rtm = d["kind"] in (ARTM, QRTM)
+        if rtm:
+            nx, nz = d["nxx"] - 2 * d["pml"], d["nzz"] - 2 * d["pml"]
+            obs = np.ascontiguousarray(obs, dtype=np.float32)
+            out0 = np.zeros((nx, nz), dtype=np.float32)
+            out1 = np.zeros((nx, nz), dtype=np.float32)
+        else:
+            out0 = np.zeros((d["nt"], D.s.nr), dtype=np.float32)
+            out1 = None
+        rid = int(lib().qpstd_server_submit(self.h, C.byref(D.s), _f(obs), _f(out0), _f(out1)))
+        if rid < 0:
+            _check(rid)
+        self.keep[rid] = (D, obs, out0, out1)
+        return rid
+
+    def status(self, rid: int):
+        lat = C.c_double()
+        sn = C.c_int()
+        st = int(lib().qpstd_server_status(self.h, rid, C.byref(lat), C.byref(sn)))
+        return st, lat.value, sn.value
+
+    def wait(self, rid: int = -1):
+        _check(lib().qpstd_server_wait(self.h, rid))
+
+    def result(self, rid: int):
+        """Gather (modeling) or (image, illumination) (RTM) of a finished request."""
+        D, obs, out0, out1 = self.keep[rid]
+        return out0 if out1 is None else (out0, out1)
+
+    def close(self):
+        if self.h:
+            lib().qpstd_server_destroy(self.h)
             self.h = C.c_void_p()
 
     def __del__(self):

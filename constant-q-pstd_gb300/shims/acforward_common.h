@@ -1,0 +1,255 @@
+// acforward_common.h -- the shared per-shot body of the reference-signature
+// acforward shims.
+//
+// The reference builds each program (aps, vaps, artm, qrtm) from a host main
+// (parameters, MPI shot distribution, model files, coefficient tables) and one
+// CUDA file whose extern "C" acforward time-steps the shots.  A shim object
+// compiled from acforward_<program>.cpp has that acforward's exact signature;
+// linked in place of the CUDA file (with libqpstd.so), the program's own main
+// and host C helpers run unchanged.  Per shot the shim does what the
+// reference's acforward does on the host -- window the models, place source and
+// receivers, write the gather / read and mute the observed data, filter, mute
+// and project the image -- and hands the time stepping to the C ABI.
+//
+// Differences: one GPU per process (GPU_N must be 1; the reference's MPI ranks
+// each own a GPU); the coefficient tables the program passes (CPML profiles,
+// shift and k-space symbols) are not read -- the library evaluates the same
+// formulas in FP64 -- except that the CPML frequency, which acforward does not
+// receive, is recovered from the interior CPML decay i_bx = exp(-dt pi fd).
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/qpstd.h"
+
+// The program's struct MultiGPU (statement.h) begins with the shot table that
+// its main fills before calling acforward; the shims read only this prefix.
+struct MultiGPU {
+    int *shotid;
+    float *sxp;
+    float *szp;
+};
+
+// Host helpers the program links (its funca.c / func.c), called as the
+// reference's acforward calls them.
+extern "C" {
+void select_part_model(int pml, float mlx, float dx, int nxt, int nzt, int nx, int nz, int nxx, int nzz, float *vpt,
+                       float *vp);
+void expand_pml_areas(int nx, int nz, int nxx, int nzz, int pml, float *vp);
+void input_geophone_pos(int shotid, int nr, float *gxp, char fname[]);
+void projectomodel(int pml, float mlx, float dx, int nxt, int nzt, int nx, int nz, int nxx, int nzz, float *vpt,
+                   float *vp);
+void removedirect(int nrmx, int tmax, int nr, float dt, float fd, float xs, float zs, float *gxp, float *gzp,
+                  float v0, float *recsim);
+float get_max_tao(int nxx, int nzz, float *tao);
+}
+
+namespace qpshim {
+
+// The grid, model and geometry arguments every acforward receives.
+struct Common {
+    int tmax;
+    float dt;
+    float *rik;
+    int myid;
+    float *gxp, *gzp;
+    int nrmx, nx, nz, nxx, nzz, pml;
+    float dx, dz, sroffmx, disx;
+    int nxt, nzt;
+    int *tracenum;
+    float *i_bx;
+    char *fname4, *fname5;
+};
+
+// One shot on its window (sgpstd-qmodeling/acps4.cu:312-430).
+struct Shot {
+    int shotid = 0, nr = 0, xsg = 0, zsg = 0, lgest = 10000, rgest = -1;
+    float xs = 0.f, zs = 0.f, mlx = 0.f;
+    std::vector<float> f[8];  // vp, rho, bbx, bbz, gam, lam, vwd, tao
+    std::vector<int> gxg, gzg;
+};
+
+// CPML frequency from the interior decay the program computed (i_bx = exp(-dt pi fd)).
+inline float cpml_fd(const Common &c) {
+    const float b = c.i_bx[c.nxx / 2];
+    return (b > 0.f && b < 1.f) ? (float)(-std::log((double)b) / ((double)c.dt * 3.1415926)) : 0.f;
+}
+
+// Windows the given full models (null entries skipped) and places source and receivers.
+inline bool window(const Common &c, MultiGPU *singpu, int ns, float *const *models, Shot &s) {
+    s.shotid = singpu[0].shotid[ns];
+    s.xs = singpu[0].sxp[ns];
+    s.zs = singpu[0].szp[ns];
+    printf("myid=%d shotid=%d nxx=%d nzz=%d xs=%f zs=%f\n", c.myid, s.shotid, c.nxx, c.nzz, s.xs, s.zs);
+    s.mlx = s.xs - c.sroffmx - c.disx;
+    const size_t N = (size_t)c.nxx * c.nzz;
+    for (int k = 0; k < 8; k++) {
+        s.f[k].clear();
+        if (!models[k]) continue;
+        s.f[k].assign(N, 0.f);
+        select_part_model(c.pml, s.mlx, c.dx, c.nxt, c.nzt, c.nx, c.nz, c.nxx, c.nzz, models[k], s.f[k].data());
+        expand_pml_areas(c.nx, c.nz, c.nxx, c.nzz, c.pml, s.f[k].data());
+    }
+    s.zsg = (int)(s.zs / c.dz + 0.5) + c.pml;
+    s.xsg = (int)((c.sroffmx + c.disx) / c.dx + 0.5) + c.pml;
+    if (s.xsg < 0 || s.xsg >= c.nxx || s.zsg < 0 || s.zsg >= c.nzz) {
+        printf("%d shot grid index exceeds model!\n", s.shotid);
+        return false;
+    }
+    s.nr = c.tracenum[s.shotid];
+    input_geophone_pos(s.shotid, s.nr, c.gxp, c.fname4);
+    input_geophone_pos(s.shotid, s.nr, c.gzp, c.fname5);
+    s.gxg.assign(s.nr, 0);
+    s.gzg.assign(s.nr, 0);
+    s.lgest = 10000;
+    s.rgest = -1;
+    for (int i = 0; i < s.nr; i++) {
+        s.gzg[i] = (int)(c.gzp[i] / c.dz + 0.5) + c.pml;
+        if (c.gxp[i] >= s.xs) s.gxg[i] = s.xsg + (int)((c.gxp[i] - s.xs) / c.dx + 0.5);
+        else s.gxg[i] = s.xsg - (int)((s.xs - c.gxp[i]) / c.dx + 0.5);
+        if (s.gxg[i] < c.pml) {
+            printf("warning: receiver x grid index in left pml area!\n");
+            s.gxg[i] = c.pml;
+        }
+        if (s.gxg[i] >= c.nxx - c.pml) {
+            printf("warning: receiver x grid index in right pml area!\n");
+            s.gxg[i] = c.nxx - c.pml - 1;
+        }
+        s.rgest = std::max(s.rgest, s.gxg[i]);
+        s.lgest = std::min(s.lgest, s.gxg[i]);
+    }
+    return true;
+}
+
+inline qpstd_shot_desc describe(const Common &c, Shot &s, int kind, float fd) {
+    qpstd_shot_desc d;
+    memset(&d, 0, sizeof(d));
+    d.kind = kind;
+    d.method = QPSTD_FUSED;
+    d.nxx = c.nxx;
+    d.nzz = c.nzz;
+    d.pml = c.pml;
+    d.dx = c.dx;
+    d.dz = c.dz;
+    d.dt = c.dt;
+    d.fd = fd;
+    d.nt = c.tmax;
+    float **p[8] = {(float **)&d.vp, (float **)&d.rho, (float **)&d.bbx, (float **)&d.bbz,
+                    (float **)&d.gam, (float **)&d.lam, (float **)&d.vwd, (float **)&d.tao};
+    for (int k = 0; k < 8; k++) *p[k] = s.f[k].empty() ? nullptr : s.f[k].data();
+    d.rik = c.rik;
+    d.xsg = s.xsg;
+    d.zsg = s.zsg;
+    d.nr = s.nr;
+    d.gxg = s.gxg.data();
+    d.gzg = s.gzg.data();
+    return d;
+}
+
+inline void report(int rc, int shotid) {
+    if (rc) printf("shot %d: libqpstd error %d: %s\n", shotid, rc, qpstd_last_error());
+}
+
+// Modeling: gather to "../obsdata/<prefix><shotid>_<nr>.bin"; with flagout the
+// interior p of every tenth step appended to "../obsdata/<snap><shotid>_<nz>_<nx>.bin"
+// (sgpstd-qmodeling/acps4.cu:568-640).
+inline void model(const Common &c, MultiGPU *singpu, int nshot, float *const *models, int kind, int flagout,
+                  const char *recpre, const char *snappre) {
+    const float fd = cpml_fd(c);
+    for (int ns = 0; ns < nshot; ns++) {
+        Shot s;
+        if (!window(c, singpu, ns, models, s)) continue;
+        qpstd_shot_desc d = describe(c, s, kind, fd);
+        std::vector<float> gather((size_t)c.tmax * std::max(s.nr, 1), 0.f);
+        int rc = QPSTD_OK;
+        if (!flagout) {
+            rc = qpstd_model_shot(&d, gather.data(), nullptr);
+        } else {
+            char snap[128];
+            snprintf(snap, sizeof snap, "../obsdata/%s%d_%d_%d.bin", snappre, s.shotid, c.nz, c.nx);
+            FILE *fs = fopen(snap, "wb");
+            if (fs) fclose(fs);
+            qpstd_shot *h = nullptr;
+            rc = qpstd_shot_create(&d, &h);
+            std::vector<float> st((size_t)8 * c.nxx * c.nzz);
+            // steps [0], [1..10], [11..20], ...: the state after every t % 10 == 0
+            for (int t0 = 0; !rc && t0 < c.tmax;) {
+                const int n = (t0 == 0) ? 1 : std::min(10, c.tmax - t0);
+                rc = qpstd_shot_advance(h, t0, n, gather.data() + (size_t)t0 * s.nr);
+                const int tl = t0 + n - 1;
+                if (!rc && tl % 10 == 0 && !(rc = qpstd_shot_get_state(h, st.data()))) {
+                    fs = fopen(snap, "ab");
+                    for (int ix = c.pml; fs && ix < c.nxx - c.pml; ix++)
+                        fwrite(&st[(size_t)ix * c.nzz + c.pml], sizeof(float), c.nzz - 2 * c.pml, fs);
+                    if (fs) fclose(fs);
+                }
+                t0 += n;
+            }
+            qpstd_shot_destroy(h);
+        }
+        report(rc, s.shotid);
+        char name[128];
+        snprintf(name, sizeof name, "../obsdata/%s%d_%d.bin", recpre, s.shotid, s.nr);
+        FILE *fr = fopen(name, "wb");
+        if (fr) {
+            fwrite(gather.data(), sizeof(float), (size_t)c.tmax * s.nr, fr);
+            fclose(fr);
+        }
+    }
+}
+
+// RTM: observed data from "<recname><shotid>_<nr>.bin" with the direct wave
+// removed, the image filtered, muted outside the receiver aperture, projected
+// onto the model and summed into img_sp / ssg_sp (sgpstd-qrtm/acsglw.cu:409-420,
+// 1041-1079).
+inline void rtm(const Common &c, MultiGPU *singpu, int nshot, float *const *models, int kind, int snapnum,
+                float *img_sp, float *ssg_sp, float fobs, float v0, float etas, float etar, const char *recname) {
+    const float fd = cpml_fd(c);
+    const size_t NI = (size_t)c.nx * c.nz, NT = (size_t)c.nxt * c.nzt;
+    std::vector<float> img(NI), imgf(NI), ssg(NI), img_pj(NT), ssg_pj(NT);
+    for (int ns = 0; ns < nshot; ns++) {
+        Shot s;
+        if (!window(c, singpu, ns, models, s)) continue;
+        std::vector<float> obs((size_t)c.tmax * std::max(s.nr, 1), 0.f);
+        char name[256];
+        snprintf(name, sizeof name, "%s%d_%d.bin", recname, s.shotid, s.nr);
+        FILE *fr = fopen(name, "rb");
+        if (!fr || fread(obs.data(), sizeof(float), (size_t)c.tmax * s.nr, fr) != (size_t)c.tmax * s.nr)
+            printf("shot %d: cannot read %s\n", s.shotid, name);
+        if (fr) fclose(fr);
+        removedirect(c.nrmx, c.tmax, s.nr, c.dt, fobs, s.xs, s.zs, c.gxp, c.gzp, v0, obs.data());
+        qpstd_shot_desc d = describe(c, s, kind, fd);
+        d.snaps = snapnum;
+        d.etas = etas;
+        d.etar = etar;
+        if (kind == QPSTD_QRTM) d.taoc = get_max_tao(c.nxx, c.nzz, s.f[7].data());  // acsglw.cu:354-356
+        int rc = qpstd_rtm_shot(&d, obs.data(), img.data(), ssg.data());
+        if (!rc) rc = qpstd_filter_image(c.nx, c.nz, c.dx, c.dz, img.data(), imgf.data());
+        report(rc, s.shotid);
+        if (rc) continue;
+        const int lg = s.lgest - c.pml, rg = s.rgest - c.pml;
+        for (int j = 0; j < c.nz; j++) {
+            for (int i = 0; i < lg; i++) imgf[(size_t)i * c.nz + j] = 0.f;
+            for (int i = std::max(rg, 0); i < c.nx; i++) imgf[(size_t)i * c.nz + j] = 0.f;
+        }
+        std::fill(img_pj.begin(), img_pj.end(), 0.f);
+        std::fill(ssg_pj.begin(), ssg_pj.end(), 0.f);
+        projectomodel(c.pml, s.mlx, c.dx, c.nxt, c.nzt, c.nx, c.nz, c.nxx, c.nzz, img_pj.data(), imgf.data());
+        projectomodel(c.pml, s.mlx, c.dx, c.nxt, c.nzt, c.nx, c.nz, c.nxx, c.nzz, ssg_pj.data(), ssg.data());
+        for (size_t i = 0; i < NT; i++) {
+            img_sp[i] += img_pj[i];
+            ssg_sp[i] += ssg_pj[i];
+        }
+    }
+}
+
+inline bool one_gpu(int GPU_N) {
+    if (GPU_N == 1) return true;
+    printf("acforward (libqpstd): one GPU per process; GPU_N = %d is not supported\n", GPU_N);
+    return false;
+}
+
+}  // namespace qpshim

@@ -156,6 +156,39 @@ int qpstd_batch_pipeline_end(qpstd_batch *b);
 int qpstd_rtm_batch(const qpstd_shot_desc *d, int nshots, const float *const *obs, float *const *img,
                     float *const *ssg);
 
+/* Device bytes qpstd_shot_create would take for d (all buffers, RTM snapshot
+ * pool included); -1 for an invalid descriptor. */
+long long qpstd_shot_bytes(const qpstd_shot_desc *d);
+
+/* ---- serving: continuous batching of shot requests ------------------------
+ * No counterpart in the reference (its programs run a fixed shot list, one
+ * shot at a time).  A server owns one device-memory arena (mem_budget bytes;
+ * 0: 85 % of the free memory) and a worker thread that admits queued requests
+ * in arrival order while a slot (max_active; 0: 64) and memory allow, runs each
+ * admitted shot on its own stream in slices so later requests overlap with
+ * running ones, and retires finished shots.  An RTM request is given the
+ * largest revolve snapshot count, up to its d->snaps, that fits at admission;
+ * the image is the one qpstd_rtm_shot gives with that count (qpstd_server_status
+ * reports it).  A fused request whose window the fused passes cannot plan
+ * (lines longer than one CTA covers, about 2600 points) runs in the plain form. */
+typedef struct qpstd_server qpstd_server;
+int qpstd_server_create(long long mem_budget, int max_active, qpstd_server **out);
+/* Waits for every submitted request, then stops the worker. */
+int qpstd_server_destroy(qpstd_server *sv);
+/* Queues one shot; returns its request id (>= 0) or a negative status.
+ * APS / VAPS: out0 = gather nt*nr (obs, out1 unused).  ARTM / QRTM: obs =
+ * observed data nt*nr, out0 = image nx*nz, out1 = illumination nx*nz or NULL.
+ * Every array d points at, and obs / out0 / out1, must stay valid until the
+ * request is done. */
+long long qpstd_server_submit(qpstd_server *sv, const qpstd_shot_desc *d, const float *obs, float *out0,
+                              float *out1);
+/* 0 queued, 1 running, 2 done, < 0 failed (status code).  latency_s: seconds
+ * from submit to done (so far, while not done); snaps_used: the snapshot count
+ * an RTM request ran with.  Either may be NULL. */
+int qpstd_server_status(qpstd_server *sv, long long id, double *latency_s, int *snaps_used);
+/* Blocks until request id is done (id < 0: every request submitted so far). */
+int qpstd_server_wait(qpstd_server *sv, long long id);
+
 /* ---- low-rank form of the constant-Q mixed-domain symbol -----------------
  * W(x,k) = sinc(vp dt k^(1+gam)/2) k^gam sqrt(1 + dt tau k^1.01/2), sinc(u) =
  * sin(u)/u, |k| on the half grid nxh x nzh (nxh = nxx/2+1, nzh = nzz/2+1,

@@ -97,6 +97,34 @@ def main():
     out["tm_vp"], out["tm_qp"] = vp, qp
     for k, a in zip(["gam", "lam", "vwd", "tao"], tm):
         out[f"tm_{k}"] = a
+    # windowing helpers of the programs (sgpstd-qrtm/funca.c): select_part_model,
+    # expand_pml_areas, projectomodel for windows inside, across the right edge
+    # of, and left of the model; removedirect on a small gather
+    qr_a = O.ref_lib("qr_funca")
+    qr_a.select_part_model.argtypes = [C.c_int, C.c_float, C.c_float] + [C.c_int] * 6 + [fp, fp]
+    qr_a.expand_pml_areas.argtypes = [C.c_int] * 5 + [fp]
+    qr_a.projectomodel.argtypes = [C.c_int, C.c_float, C.c_float] + [C.c_int] * 6 + [fp, fp]
+    qr_a.removedirect.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, fp, fp,
+                                  C.c_float, fp]
+    nxt, nzt, pml, dxw = 50, 12, 4, 10.0
+    vpt = rng.uniform(1500.0, 4500.0, size=nxt * nzt).astype(np.float32)
+    for c, (mlx, nx) in enumerate([(55.0, 20), (402.0, 20), (-63.0, 30), (-41.0, 70)]):
+        nxx, nzz = nx + 2 * pml, nzt + 2 * pml
+        w = f32(nxx * nzz)
+        qr_a.select_part_model(pml, mlx, dxw, nxt, nzt, nx, nzt, nxx, nzz, pf(vpt), pf(w))
+        qr_a.expand_pml_areas(nx, nzt, nxx, nzz, pml, pf(w))
+        img = rng.standard_normal(nx * nzt).astype(np.float32)
+        pj = f32(nxt * nzt)
+        qr_a.projectomodel(pml, mlx, dxw, nxt, nzt, nx, nzt, nxx, nzz, pf(pj), pf(img))
+        out[f"win{c}_case"] = np.array([mlx, nx], dtype=np.float64)
+        out[f"win{c}_model"], out[f"win{c}_img"], out[f"win{c}_pj"] = w, img, pj
+    out["win_vpt"] = vpt
+    obs = rng.standard_normal(300 * 16).astype(np.float32)
+    gx = np.linspace(0.0, 600.0, 16).astype(np.float32)
+    gz = np.full(16, 20.0, dtype=np.float32)
+    out["rd_in"] = obs.copy()
+    qr_a.removedirect(16, 300, 16, 0.001, 25.0, 250.0, 20.0, pf(gx), pf(gz), 1800.0, pf(obs))
+    out["rd_out"] = obs
     for steps, snaps in REVOLVE:
         check, capo, fine, info = C.c_int(-1), C.c_int(0), C.c_int(steps), C.c_int(0)
         tr = []

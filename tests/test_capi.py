@@ -37,3 +37,21 @@ def test_python_bindings_cover_the_header():
 
 def test_version_without_gpu():
     assert qpstd.lib().qpstd_version() >= 100
+
+
+def test_shot_bytes_grows_by_the_snapshot_pool():
+    """Host-only estimate (no GPU): each RTM snapshot holds 8 fields of N floats."""
+    import workloads as W
+    d = W.make_shot(qpstd.QRTM, 60, 40, 10, 50, 0.001, 25.0, seed=3, snaps=4)
+    n = d["nxx"] * d["nzz"]
+    b4 = qpstd.shot_bytes(d)
+    b9 = qpstd.shot_bytes(dict(d, snaps=9))
+    assert b9 - b4 == 5 * 32 * n
+    assert qpstd.shot_bytes(dict(d, kind=qpstd.VAPS)) < b4
+
+
+def test_shot_bytes_marks_windows_the_fused_passes_cannot_plan():
+    import workloads as W
+    d = W.make_shot(qpstd.APS, 4096, 24, 10, 40, 0.0005, 25.0, seed=9)
+    assert qpstd.shot_bytes(d) == -1
+    assert qpstd.shot_bytes(dict(d, method=qpstd.PLAIN)) > 0

@@ -1,0 +1,120 @@
+"""Serving (qpstd_server): continuous batching of shot requests.
+
+Each request's result in a mix equals its result alone (the direct C ABI on
+the same descriptor, with the snapshot count the server gave it) within
+relative L2 1e-6: the serving path changes scheduling only.  The snapshot
+count itself does change an RTM image slightly, as in the reference: a restore
+from checkpoint 0 resumes at step 1 with the first source sample already in the
+state (sgpstd-qrtm/acsglw.cu:493-500,1008), and how often that restore happens
+depends on the schedule.  Requests arrive while others run, under a memory
+budget small enough to force queuing and a lowered snapshot count.
+"""
+import time
+
+import numpy as np
+import pytest
+
+import qpstd
+import workloads as W
+from cases import rel_l2
+
+TOL = 1e-6
+
+
+def _mix():
+    shots = [
+        W.make_shot(qpstd.APS, 70, 40, 10, 160, 0.001, 25.0, seed=501),
+        W.make_shot(qpstd.VAPS, 57, 33, 10, 150, 0.001, 25.0, seed=502),
+        W.make_shot(qpstd.ARTM, 83, 45, 10, 140, 0.001, 25.0, seed=503, snaps=8),
+        W.make_shot(qpstd.QRTM, 64, 38, 10, 150, 0.001, 25.0, seed=504, snaps=6),
+        W.make_shot(qpstd.APS, 101, 64, 12, 120, 0.001, 25.0, seed=505),
+        W.make_shot(qpstd.QRTM, 90, 51, 10, 130, 0.001, 25.0, seed=506, snaps=10),
+    ]
+    obs = []
+    for d in shots:
+        if d["kind"] in (qpstd.ARTM, qpstd.QRTM):
+            md = dict(d, kind=qpstd.APS if d["kind"] == qpstd.ARTM else qpstd.VAPS)
+            obs.append(qpstd.model_shot(md))
+        else:
+            obs.append(None)
+    return shots, obs
+
+
+def _alone(d, o):
+    if o is None:
+        return qpstd.model_shot(d)
+    return qpstd.rtm_shot(d, o)
+
+
+def _same(a, b):
+    if isinstance(a, tuple):
+        return rel_l2(a[0], b[0]) <= TOL and rel_l2(a[1], b[1]) <= TOL
+    return rel_l2(a, b) <= TOL
+
+
+@pytest.mark.gpu
+def test_server_mix_equals_alone():
+    shots, obs = _mix()
+    ref = [_alone(d, o) for d, o in zip(shots, obs)]
+    sv = qpstd.Server(mem_budget=0, max_active=4)
+    ids = []
+    for i, (d, o) in enumerate(zip(shots, obs)):
+        ids.append(sv.submit(d, o))
+        if i == 2:
+            time.sleep(0.05)  # later requests arrive while the first ones run
+    sv.wait()
+    for rid, r, d, o in zip(ids, ref, shots, obs):
+        st, lat, snaps = sv.status(rid)
+        assert st == 2 and lat > 0
+        if o is not None and snaps != d["snaps"]:
+            r = _alone(dict(d, snaps=snaps), o)
+        assert _same(sv.result(rid), r)
+    sv.close()
+
+
+@pytest.mark.gpu
+def test_server_small_budget_queues_and_lowers_snapshots():
+    shots, obs = _mix()
+    d, o = shots[5], obs[5]               # Q-RTM, 10 snapshots requested
+    ref = _alone(dict(d, snaps=4), o)
+    base = qpstd.shot_bytes(dict(d, snaps=0))
+    per_snap = 32 * d["nxx"] * d["nzz"]
+    budget = base + 4 * per_snap + per_snap // 2    # room for 4 snapshots
+    sv = qpstd.Server(mem_budget=budget, max_active=8)
+    rid = sv.submit(d, o)
+    rid2 = sv.submit(shots[0], None)      # queued behind it if memory is short
+    sv.wait()
+    st, _, snaps = sv.status(rid)
+    assert st == 2 and snaps == 4
+    assert _same(sv.result(rid), ref)
+    assert sv.status(rid2)[0] == 2
+    assert _same(sv.result(rid2), _alone(shots[0], None))
+    sv.close()
+
+
+@pytest.mark.gpu
+def test_shot_bytes_covers_the_allocation():
+    import torch
+    d = W.make_shot(qpstd.QRTM, 560, 300, 20, 400, 0.001, 20.0, seed=7, snaps=12)
+    torch.cuda.init()
+    torch.cuda.synchronize()
+    f0 = torch.cuda.mem_get_info()[0]
+    sh = qpstd.Shot(d)
+    torch.cuda.synchronize()
+    used = f0 - torch.cuda.mem_get_info()[0]
+    est = qpstd.shot_bytes(d)
+    sh.close()
+    assert est >= 0.9 * used and est <= 1.3 * used + 8 * 2**20, (est, used)
+
+
+@pytest.mark.gpu
+def test_server_serves_windows_beyond_the_fused_lines_in_plain_form():
+    d = W.make_shot(qpstd.APS, 4096, 24, 10, 40, 0.0005, 25.0, seed=9)   # padded width 4117
+    assert qpstd.shot_bytes(d) < 0 <= qpstd.shot_bytes(dict(d, method=qpstd.PLAIN))
+    ref = qpstd.model_shot(d, method=qpstd.PLAIN)
+    sv = qpstd.Server(max_active=2)
+    rid = sv.submit(d)
+    sv.wait()
+    assert sv.status(rid)[0] == 2
+    assert rel_l2(sv.result(rid), ref) <= TOL
+    sv.close()

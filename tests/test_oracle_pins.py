@@ -105,3 +105,36 @@ def test_live_reference_objects_if_built():
             if a in (5, 6):
                 break
         assert (np.array(tr) == O.revolve_trace(steps, snaps)).all()
+
+
+def test_host_helpers_pinned():
+    """The C restatement of the programs' windowing helpers (oracle/host_helpers.c,
+    linked by the acforward shim harness) against the reference's compiled ones."""
+    import ctypes as C
+    L = O.lib()
+    fp = C.POINTER(C.c_float)
+    L.select_part_model.argtypes = [C.c_int, C.c_float, C.c_float] + [C.c_int] * 6 + [fp, fp]
+    L.expand_pml_areas.argtypes = [C.c_int] * 5 + [fp]
+    L.projectomodel.argtypes = [C.c_int, C.c_float, C.c_float] + [C.c_int] * 6 + [fp, fp]
+    L.removedirect.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, fp, fp,
+                               C.c_float, fp]
+    pf = lambda a: a.ctypes.data_as(fp)
+    vpt = GOLD["win_vpt"]
+    nxt, nzt, pml, dxw = 50, 12, 4, 10.0
+    for c in range(4):
+        mlx, nx = GOLD[f"win{c}_case"]
+        nx = int(nx)
+        nxx, nzz = nx + 2 * pml, nzt + 2 * pml
+        w = np.zeros(nxx * nzz, dtype=np.float32)
+        L.select_part_model(pml, mlx, dxw, nxt, nzt, nx, nzt, nxx, nzz, pf(vpt), pf(w))
+        L.expand_pml_areas(nx, nzt, nxx, nzz, pml, pf(w))
+        assert np.array_equal(w, GOLD[f"win{c}_model"]), c
+        pj = np.zeros(nxt * nzt, dtype=np.float32)
+        img = np.ascontiguousarray(GOLD[f"win{c}_img"])
+        L.projectomodel(pml, mlx, dxw, nxt, nzt, nx, nzt, nxx, nzz, pf(pj), pf(img))
+        assert np.array_equal(pj, GOLD[f"win{c}_pj"]), c
+    obs = np.array(GOLD["rd_in"])
+    gx = np.linspace(0.0, 600.0, 16).astype(np.float32)
+    gz = np.full(16, 20.0, dtype=np.float32)
+    L.removedirect(16, 300, 16, 0.001, 25.0, 250.0, 20.0, pf(gx), pf(gz), 1800.0, pf(obs))
+    assert np.array_equal(obs, GOLD["rd_out"])
