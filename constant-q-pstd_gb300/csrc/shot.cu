@@ -622,6 +622,41 @@ static void plain_one(qpstd_shot* s, Wave& w, float src, int t_filter, float eta
     if (rc && !s->plain_err) s->plain_err = rc;
 }
 
+// The Q-RTM stabilised symbol S = ka - 2 eta ka (1 + tau dt ka) / (exp(-tau tt ka)
+// + eta exp(tau dt ka)) (multt_kernel, sgpstd-qrtm/acsglw.cu:1895, float
+// arithmetic, tt = t dt) rounds to ka itself while its correction stays below a
+// quarter ulp of ka, which with the reference's eta ~ 1e-26 holds for every
+// step of ordinary runs.  The correction grows with tt, so per eta the largest
+// such step is found once (over 4096 samples of ka up to the grid's largest);
+// steps up to it use the k^1.01 operator -- the per-kz convolution when the
+// width needs Bluestein -- instead of exact transforms.
+static bool filter_is_ka(qpstd_shot* s, float eta, int t) {
+    for (auto& c : s->ka_steps)
+        if (c.first == eta) return t <= c.second;
+    const double kx = wavenumber(s->d.nxx / 2, s->d.nxx, s->d.dx), kz = wavenumber(s->d.nzz / 2, s->d.nzz, s->d.dz);
+    const double kmax2 = kx * kx + kz * kz;  // the largest |k|^2 of the grid
+    const double e6 = (double)eta * 1e-6, tau = s->d.taoc, dt = s->d.dt;
+    auto plain_at = [&](int tt_idx) {
+        const double tt = (double)tt_idx * dt;
+        for (int i = 1; i <= 4096; i++) {
+            const double ka = std::pow(kmax2 * i / 4096.0, 0.505);
+            const double corr = 2.0 * e6 * (1.0 + tau * dt * ka) / (std::exp(-tau * tt * ka) + e6 * std::exp(tau * dt * ka));
+            if (!(corr < std::ldexp(1.0, -26))) return false;
+        }
+        return true;
+    };
+    int lo = -1, hi = s->d.nt;  // plain_at(lo) holds (or lo = -1), plain_at(hi) is never asked
+    if (plain_at(s->d.nt)) lo = s->d.nt;
+    else
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) / 2;
+            if (plain_at(mid)) lo = mid;
+            else hi = mid;
+        }
+    s->ka_steps.push_back({eta, lo});
+    return t <= lo;
+}
+
 // One constant-Q step of wavefield w (seven launches, see vz_kernels.cu).
 // src: amplitude at the source this step; t_filter / eta: time index and
 // stabilisation of the Q-RTM aux filter; last: skip the next step's Dx;
@@ -705,7 +740,7 @@ static void vz_step(qpstd_shot* s, Wave& w, float src, int t_filter, float eta, 
         VxsArgs a = xs;
         a.L = s->Lxs;
         a.in = s->spec[2]; a.out0 = w.aux_spec;
-        if (s->d.kind == QPSTD_QRTM) {
+        if (s->d.kind == QPSTD_QRTM && !(s->xconv && filter_is_ka(s, eta, t_filter))) {
             // multt_kernel, sgpstd-qrtm/acsglw.cu:1895: eta scaled by 1e-6, tt = nt*dt in float
             a.mode = 2; a.eta6 = (float)((double)eta * 1e-6); a.tao = s->d.taoc; a.dt = s->d.dt;
             a.tt = (float)t_filter * s->d.dt;
@@ -788,10 +823,18 @@ static void src_end(qpstd_shot* s) {
 // other, keeping the fastest.  Results are cached per grid shape for the
 // process.  QPSTD_AUTOTUNE=0 keeps the built-in choice.
 namespace {
+// One tuned kernel family: its lines per CTA and, for the acoustic passes,
+// whether the epilogue inputs are staged in shared memory (staging hides
+// their loads behind the transforms but takes shared memory that would hold
+// more resident CTAs).
 struct Knob {
     int* L;
-    int lmax;
     bool pow2;
+    int tx;              // threads per line
+    size_t per_line;     // shared bytes per line without staging
+    size_t budget;       // shared bytes the kernel may use
+    bool* stage = nullptr;
+    size_t stage_bytes = 0;  // extra shared bytes per line when staging
 };
 std::mutex g_tune_mu;
 std::map<std::vector<int>, std::vector<int>> g_tune_cache;
@@ -823,25 +866,28 @@ static int autotune(qpstd_shot* s) {
     if (s->d.method != QPSTD_FUSED || (env && env[0] == '0')) return QPSTD_OK;
     const size_t stz = (size_t)40 * s->d.nzz, stx = (size_t)72 * s->d.nxx;
     std::vector<Knob> knobs;
+    const size_t vzb = 160 * 1024, acb = QP_SMEM_DYN_MAX;
     if (s->visco) {
         const int mz = std::max(s->pz.m, s->pzc.m), tz = std::max(s->pz.tx, s->pzc.tx);
         const FFTPlanDev& pxs = s->xconv ? s->pxc : s->px;
-        knobs.push_back({&s->Lzv, lmax_of(tz, (size_t)16 * mz, 160 * 1024), false});
-        knobs.push_back({&s->Lxs3, lmax_of(pxs.tx, (size_t)16 * pxs.m, 160 * 1024), true});
-        knobs.push_back({&s->Lxs, lmax_of(pxs.tx, (size_t)8 * pxs.m, 160 * 1024), true});
-        if (s->xconv && s->d.kind == QPSTD_QRTM)
-            knobs.push_back({&s->Lxs_exact, lmax_of(s->px.tx, (size_t)8 * s->px.m, 160 * 1024), true});
+        knobs.push_back({&s->Lzv, false, tz, (size_t)16 * mz, vzb});
+        knobs.push_back({&s->Lxs3, true, pxs.tx, (size_t)16 * pxs.m, vzb});
+        knobs.push_back({&s->Lxs, true, pxs.tx, (size_t)8 * pxs.m, vzb});
+        if (s->xconv && s->d.kind == QPSTD_QRTM) knobs.push_back({&s->Lxs_exact, true, s->px.tx, (size_t)8 * s->px.m, vzb});
     } else {
-        knobs.push_back({&s->Lzp, lmax_of(s->pzc.tx, (size_t)8 * s->pzc.m + (s->stage_z ? stz : 0), QP_SMEM_DYN_MAX),
-                         false});
+        knobs.push_back({&s->Lzp, false, s->pzc.tx, (size_t)8 * s->pzc.m, acb, &s->stage_z, stz});
     }
-    knobs.push_back({&s->Lx, lmax_of(s->pxc.tx, (size_t)8 * s->pxc.m + (s->stage_x ? stx : 0), QP_SMEM_DYN_MAX), true});
+    knobs.push_back({&s->Lx, true, s->pxc.tx, (size_t)8 * s->pxc.m, acb, &s->stage_x, stx});
+    // cached per shape: L * 2 + staging
     const std::vector<int> key = {s->d.kind, s->d.nxx, s->d.nzz};
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune_cache.find(key);
         if (it != g_tune_cache.end() && it->second.size() == knobs.size()) {
-            for (size_t i = 0; i < knobs.size(); i++) *knobs[i].L = it->second[i];
+            for (size_t i = 0; i < knobs.size(); i++) {
+                *knobs[i].L = it->second[i] >> 1;
+                if (knobs[i].stage) *knobs[i].stage = it->second[i] & 1;
+            }
             return QPSTD_OK;
         }
     }
@@ -852,29 +898,37 @@ static int autotune(qpstd_shot* s) {
     const bool prof = s->prof;
     s->prof = false;
     for (Knob& k : knobs) {
-        const int cur = *k.L;
-        std::vector<int> cand = {cur};
-        for (int L : {1, 2, 3, 4, 6, 8, 12, 16})
-            if (L <= k.lmax && L != cur && (!k.pow2 || (L & (L - 1)) == 0)) cand.push_back(L);
-        int best = cur;
+        // (staging, L) pairs: the current one first, then every admissible one
+        std::vector<std::pair<int, int>> cand = {{k.stage ? (int)*k.stage : 0, *k.L}};
+        for (int st = 0; st <= (k.stage ? 1 : 0); st++) {
+            const size_t per = k.per_line + (st ? k.stage_bytes : 0);
+            if (per > k.budget) continue;  // staging does not fit beside one line
+            const int lmax = lmax_of(k.tx, per, k.budget);
+            for (int L : {1, 2, 3, 4, 6, 8, 12, 16})
+                if (L <= lmax && (!k.pow2 || (L & (L - 1)) == 0) && std::make_pair(st, L) != cand[0])
+                    cand.push_back({st, L});
+        }
+        std::pair<int, int> best = cand[0];
         float tbest = 1e30f;
-        for (int L : cand) {
-            *k.L = L;
+        for (const auto& c : cand) {
+            if (k.stage) *k.stage = c.first != 0;
+            *k.L = c.second;
             float t = time_steps(s, 1, 3);
             t = std::min(t, time_steps(s, 0, 3));
             if (t > 0.f && t < tbest) {
                 tbest = t;
-                best = L;
+                best = c;
             }
         }
-        *k.L = best;
+        if (k.stage) *k.stage = best.first != 0;
+        *k.L = best.second;
     }
     s->prof = prof;
     cudaError_t e = cudaStreamSynchronize(s->stream);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "autotune");
     std::vector<int> val;
-    for (Knob& k : knobs) val.push_back(*k.L);
+    for (Knob& k : knobs) val.push_back(*k.L * 2 + (k.stage && *k.stage ? 1 : 0));
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune_cache[key] = val;
     return QPSTD_OK;

@@ -92,6 +92,8 @@ struct qpstd_shot {
     // (k^2)^(33/32), (k^2)^0.505
     bool xconv = false;
     const float* xtab[4] = {nullptr, nullptr, nullptr, nullptr};
+    // Q-RTM filter: per eta, the last step at which it rounds to k^1.01 (see filter_is_ka)
+    std::vector<std::pair<float, int>> ka_steps;
     int* rec_off_z = nullptr;                // receivers keyed by z-pass tile
     qp::RecEntry* rec_z = nullptr;
     // plain (cuFFT) form
