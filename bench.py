@@ -401,6 +401,9 @@ def main():
         qpstd.lib().qpstd_shot_set_profiling(B.shot(i), 1)
     launches0 = sum(int(qpstd.lib().qpstd_shot_launch_count(B.shot(i))) for i in range(len(shots)))
     step_ms = []
+    # the timed steps are the profiler's range (ncu --profile-from-start off
+    # skips shot creation and tuning)
+    torch.cuda.profiler.start()
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
         for i in range(args.steps):
@@ -418,6 +421,7 @@ def main():
             torch.cuda.synchronize()
             step_ms.append(max(e0.elapsed_time(e) for e in ends))
             t += 1
+    torch.cuda.profiler.stop()
     launches = sum(int(qpstd.lib().qpstd_shot_launch_count(B.shot(i))) for i in range(len(shots))) - launches0
     kern = {}
     for i in range(len(shots)):

@@ -1280,3 +1280,30 @@ extern "C" int qpstd_filter_image(int nx, int nz, float dx, float dz, const floa
     if (e != cudaSuccess) return cuda_fail(e, "filter_image");
     return QPSTD_OK;
 }
+
+// Source-normalised imaging condition r / (s + sigma^2): the reference
+// accumulates the cross-correlation r (img_sp) and the source illumination s
+// (ssg_sp) and leaves the division to the user; the stabilisation sigma^2 keeps
+// unilluminated points finite.
+__global__ void normalize_image_kernel(size_t n, float sigma2, const float* __restrict__ img,
+                                       const float* __restrict__ ssg, float* __restrict__ out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = img[i] / (ssg[i] + sigma2);
+}
+
+extern "C" int qpstd_normalize_image(int nx, int nz, float sigma2, const float* img, const float* ssg, float* out) {
+    if (nx < 1 || nz < 1 || !img || !ssg || !out) return fail(QPSTD_EINVAL, "bad normalisation arguments");
+    const size_t n = (size_t)nx * nz;
+    float* a = nullptr;
+    CK(cudaMalloc(&a, 12 * n));
+    cudaError_t e = cudaMemcpy(a, img, 4 * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(a + n, ssg, 4 * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        normalize_image_kernel<<<(unsigned)((n + 255) / 256), 256>>>(n, sigma2, a, a + n, a + 2 * n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, a + 2 * n, 4 * n, cudaMemcpyDeviceToHost);
+    cudaFree(a);
+    if (e != cudaSuccess) return cuda_fail(e, "normalize_image");
+    return QPSTD_OK;
+}

@@ -57,6 +57,7 @@ EXPORTS = {
     "qpstd_model_shot": (C.c_int, [C.POINTER(ShotDesc), _fp, _fp]),
     "qpstd_rtm_shot": (C.c_int, [C.POINTER(ShotDesc), _fp, _fp, _fp]),
     "qpstd_filter_image": (C.c_int, [C.c_int, C.c_int, C.c_float, C.c_float, _fp, _fp]),
+    "qpstd_normalize_image": (C.c_int, [C.c_int, C.c_int, C.c_float, _fp, _fp, _fp]),
     "qpstd_shot_create": (C.c_int, [C.POINTER(ShotDesc), C.POINTER(C.c_void_p)]),
     "qpstd_shot_destroy": (C.c_int, [C.c_void_p]),
     "qpstd_shot_set_state": (C.c_int, [C.c_void_p, _fp]),
@@ -178,6 +179,14 @@ def filter_image(img: np.ndarray, dx: float, dz: float) -> np.ndarray:
     img = np.ascontiguousarray(img, dtype=np.float32)
     out = np.zeros_like(img)
     _check(lib().qpstd_filter_image(img.shape[0], img.shape[1], dx, dz, _f(img), _f(out)))
+    return out
+
+
+def normalize_image(img: np.ndarray, ssg: np.ndarray, sigma2: float = 1e-26) -> np.ndarray:
+    img = np.ascontiguousarray(img, dtype=np.float32)
+    ssg = np.ascontiguousarray(ssg, dtype=np.float32)
+    out = np.zeros_like(img)
+    _check(lib().qpstd_normalize_image(img.shape[0], img.shape[1], sigma2, _f(img), _f(ssg), _f(out)))
     return out
 
 

@@ -87,6 +87,11 @@ int qpstd_rtm_shot(const qpstd_shot_desc *d, const float *obs, float *img, float
  * writes are not reproduced).  img, imgf: host nx*nz. */
 int qpstd_filter_image(int nx, int nz, float dx, float dz, const float *img, float *imgf);
 
+/* Source-normalised imaging condition out = img / (ssg + sigma2) on the
+ * device (host nx*nz arrays): the reference leaves this step to the user after
+ * summing img_sp / ssg_sp; sigma2 is the stabilisation (e.g. 1e-26). */
+int qpstd_normalize_image(int nx, int nz, float sigma2, const float *img, const float *ssg, float *out);
+
 /* ---- device-resident shot handle (inputs stay in HBM between calls) ---- */
 typedef struct qpstd_shot qpstd_shot;
 

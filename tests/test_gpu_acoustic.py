@@ -61,3 +61,12 @@ def test_artm_small_shot_image():
     img, ssg = qpstd.rtm_shot(d, obs)
     assert rel_l2(ssg, ref_ssg) < TOL
     assert rel_l2(img, ref_img) < TOL
+    # the post-processing chain: Laplacian filter, then r / (s + sigma^2)
+    imgf = qpstd.filter_image(img, d["dx"], d["dz"])
+    ref_f = O.filter_image(ref_img, d["dx"], d["dz"])
+    assert rel_l2(imgf, ref_f) < TOL
+    sig = 1e-26
+    norm = qpstd.normalize_image(imgf, ssg, sig)
+    lit = ref_ssg > 1e-3 * ref_ssg.max()  # where the source illuminates (the ratio is stable)
+    assert rel_l2(norm[lit], (ref_f / (ref_ssg + sig))[lit]) < TOL
+    assert np.array_equal(norm, imgf / (ssg + np.float32(sig)))
