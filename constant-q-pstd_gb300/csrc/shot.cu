@@ -861,23 +861,56 @@ static float time_steps(qpstd_shot* s, int warm, int n) {
     return ms;
 }
 
-static int autotune(qpstd_shot* s) {
-    const char* env = getenv("QPSTD_AUTOTUNE");
-    if (s->d.method != QPSTD_FUSED || (env && env[0] == '0')) return QPSTD_OK;
+// The tuned kernel families of a shot.
+static std::vector<Knob> shot_knobs(qpstd_shot* s) {
     const size_t stz = (size_t)40 * s->d.nzz, stx = (size_t)72 * s->d.nxx;
     std::vector<Knob> knobs;
     const size_t vzb = 160 * 1024, acb = QP_SMEM_DYN_MAX;
     if (s->visco) {
         const int mz = std::max(s->pz.m, s->pzc.m), tz = std::max(s->pz.tx, s->pzc.tx);
         const FFTPlanDev& pxs = s->xconv ? s->pxc : s->px;
-        knobs.push_back({&s->Lzv, false, tz, (size_t)16 * mz, vzb});
+        knobs.push_back({&s->Lzv, false, tz, (size_t)16 * mz, vzb});  // z passes A-C share L
         knobs.push_back({&s->Lxs3, true, pxs.tx, (size_t)16 * pxs.m, vzb});
         knobs.push_back({&s->Lxs, true, pxs.tx, (size_t)8 * pxs.m, vzb});
-        if (s->xconv && s->d.kind == QPSTD_QRTM) knobs.push_back({&s->Lxs_exact, true, s->px.tx, (size_t)8 * s->px.m, vzb});
+        if (s->xconv && s->d.kind == QPSTD_QRTM)
+            knobs.push_back({&s->Lxs_exact, true, s->px.tx, (size_t)8 * s->px.m, vzb});
     } else {
         knobs.push_back({&s->Lzp, false, s->pzc.tx, (size_t)8 * s->pzc.m, acb, &s->stage_z, stz});
     }
     knobs.push_back({&s->Lx, true, s->pxc.tx, (size_t)8 * s->pxc.m, acb, &s->stage_x, stx});
+    return knobs;
+}
+
+// Admissible (staging, L) pairs of a knob.
+static std::vector<std::pair<int, int>> knob_pairs(const Knob& k) {
+    std::vector<std::pair<int, int>> out;
+    for (int st = 0; st <= (k.stage ? 1 : 0); st++) {
+        const size_t per = k.per_line + (st ? k.stage_bytes : 0);
+        if (per > k.budget) continue;  // staging does not fit beside one line
+        const int lmax = lmax_of(k.tx, per, k.budget);
+        for (int L : {1, 2, 3, 4, 6, 8, 12, 16})
+            if (L <= lmax && (!k.pow2 || (L & (L - 1)) == 0)) out.push_back({st, L});
+    }
+    return out;
+}
+
+static void knob_set(const Knob& k, std::pair<int, int> c) {
+    if (k.stage) *k.stage = c.first != 0;
+    *k.L = c.second;
+}
+
+// Zero state and scratch spectra (cudaMalloc leaves them undefined) so that
+// tuning steps keep every field zero.
+static void tune_prepare(qpstd_shot* s) {
+    for (int k = 0; k < 4; k++)
+        if (s->spec[k]) cudaMemsetAsync(s->spec[k], 0, sizeof(float2) * (size_t)s->d.nxx * s->nzh, s->stream);
+    cudaMemsetAsync(s->src.st, 0, sizeof(float) * 9 * s->N, s->stream);
+}
+
+static int autotune(qpstd_shot* s) {
+    const char* env = getenv("QPSTD_AUTOTUNE");
+    if (s->d.method != QPSTD_FUSED || (env && env[0] == '0')) return QPSTD_OK;
+    std::vector<Knob> knobs = shot_knobs(s);
     // cached per shape: L * 2 + staging
     const std::vector<int> key = {s->d.kind, s->d.nxx, s->d.nzz};
     {
@@ -891,28 +924,18 @@ static int autotune(qpstd_shot* s) {
             return QPSTD_OK;
         }
     }
-    // scratch spectra hold whatever cudaMalloc left: clear them so the zero state stays zero
-    for (int k = 0; k < 4; k++)
-        if (s->spec[k]) cudaMemsetAsync(s->spec[k], 0, sizeof(float2) * (size_t)s->d.nxx * s->nzh, s->stream);
-    cudaMemsetAsync(s->src.st, 0, sizeof(float) * 9 * s->N, s->stream);
+    tune_prepare(s);
     const bool prof = s->prof;
     s->prof = false;
     for (Knob& k : knobs) {
-        // (staging, L) pairs: the current one first, then every admissible one
+        // the current (staging, L) first, then every other admissible pair
         std::vector<std::pair<int, int>> cand = {{k.stage ? (int)*k.stage : 0, *k.L}};
-        for (int st = 0; st <= (k.stage ? 1 : 0); st++) {
-            const size_t per = k.per_line + (st ? k.stage_bytes : 0);
-            if (per > k.budget) continue;  // staging does not fit beside one line
-            const int lmax = lmax_of(k.tx, per, k.budget);
-            for (int L : {1, 2, 3, 4, 6, 8, 12, 16})
-                if (L <= lmax && (!k.pow2 || (L & (L - 1)) == 0) && std::make_pair(st, L) != cand[0])
-                    cand.push_back({st, L});
-        }
+        for (const auto& c : knob_pairs(k))
+            if (c != cand[0]) cand.push_back(c);
         std::pair<int, int> best = cand[0];
         float tbest = 1e30f;
         for (const auto& c : cand) {
-            if (k.stage) *k.stage = c.first != 0;
-            *k.L = c.second;
+            knob_set(k, c);
             float t = time_steps(s, 1, 3);
             t = std::min(t, time_steps(s, 0, 3));
             if (t > 0.f && t < tbest) {
@@ -920,8 +943,7 @@ static int autotune(qpstd_shot* s) {
                 best = c;
             }
         }
-        if (k.stage) *k.stage = best.first != 0;
-        *k.L = best.second;
+        knob_set(k, best);
     }
     s->prof = prof;
     cudaError_t e = cudaStreamSynchronize(s->stream);
