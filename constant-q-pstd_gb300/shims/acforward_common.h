@@ -19,8 +19,13 @@
 #pragma once
 #include <algorithm>
 #include <cmath>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/qpstd.h"
@@ -62,6 +67,7 @@ struct Common {
     int *tracenum;
     float *i_bx;
     char *fname4, *fname5;
+    float fd = 0.f;  // CPML frequency when known (the native programs); 0: recovered from i_bx
 };
 
 // One shot on its window (sgpstd-qmodeling/acps4.cu:312-430).
@@ -74,6 +80,7 @@ struct Shot {
 
 // CPML frequency from the interior decay the program computed (i_bx = exp(-dt pi fd)).
 inline float cpml_fd(const Common &c) {
+    if (c.fd > 0.f || !c.i_bx) return c.fd;
     const float b = c.i_bx[c.nxx / 2];
     return (b > 0.f && b < 1.f) ? (float)(-std::log((double)b) / ((double)c.dt * 3.1415926)) : 0.f;
 }
@@ -153,51 +160,110 @@ inline void report(int rc, int shotid) {
     if (rc) printf("shot %d: libqpstd error %d: %s\n", shotid, rc, qpstd_last_error());
 }
 
+// Appends float records to files on a background thread, so that snapshot
+// writes overlap the next steps on the GPU.  The destructor drains the queue.
+class AsyncWriter {
+public:
+    AsyncWriter() : th_([this] { run(); }) {}
+    ~AsyncWriter() {
+        {
+            std::lock_guard<std::mutex> g(m_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        th_.join();
+    }
+    void append(const std::string &path, std::vector<float> rec) {
+        {
+            std::lock_guard<std::mutex> g(m_);
+            q_.push_back({path, std::move(rec)});
+        }
+        cv_.notify_all();
+    }
+
+private:
+    void run() {
+        for (;;) {
+            std::pair<std::string, std::vector<float>> job;
+            {
+                std::unique_lock<std::mutex> g(m_);
+                cv_.wait(g, [this] { return stop_ || !q_.empty(); });
+                if (q_.empty()) return;
+                job = std::move(q_.front());
+                q_.pop_front();
+            }
+            FILE *f = fopen(job.first.c_str(), "ab");
+            if (f) {
+                fwrite(job.second.data(), sizeof(float), job.second.size(), f);
+                fclose(f);
+            }
+        }
+    }
+    std::mutex m_;
+    std::condition_variable cv_;
+    std::deque<std::pair<std::string, std::vector<float>>> q_;
+    bool stop_ = false;
+    std::thread th_;
+};
+
+// Gather of a modeled shot to "../obsdata/<prefix><shotid>_<nr>.bin" (time-major nt x nr).
+inline void write_gather(const Common &c, const Shot &s, const float *gather, const char *recpre) {
+    char name[256];
+    snprintf(name, sizeof name, "../obsdata/%s%d_%d.bin", recpre, s.shotid, s.nr);
+    FILE *fr = fopen(name, "wb");
+    if (!fr) {
+        printf("shot %d: cannot write %s\n", s.shotid, name);
+        return;
+    }
+    fwrite(gather, sizeof(float), (size_t)c.tmax * s.nr, fr);
+    fclose(fr);
+}
+
+// One modeled shot with the interior p of every tenth step appended to
+// "../obsdata/<snap><shotid>_<nz>_<nx>.bin" (sgpstd-qmodeling/acps4.cu:624-640).
+inline int model_with_snapshots(const Common &c, const Shot &s, const qpstd_shot_desc &d, float *gather,
+                                const char *snappre, AsyncWriter &wr) {
+    char snap[256];
+    snprintf(snap, sizeof snap, "../obsdata/%s%d_%d_%d.bin", snappre, s.shotid, c.nz, c.nx);
+    FILE *fs = fopen(snap, "wb");
+    if (fs) fclose(fs);
+    qpstd_shot *h = nullptr;
+    int rc = qpstd_shot_create(&d, &h);
+    std::vector<float> st((size_t)8 * c.nxx * c.nzz);
+    // steps [0], [1..10], [11..20], ...: the state after every t % 10 == 0
+    for (int t0 = 0; !rc && t0 < c.tmax;) {
+        const int n = (t0 == 0) ? 1 : std::min(10, c.tmax - t0);
+        rc = qpstd_shot_advance(h, t0, n, gather + (size_t)t0 * s.nr);
+        const int tl = t0 + n - 1;
+        if (!rc && tl % 10 == 0 && !(rc = qpstd_shot_get_state(h, st.data()))) {
+            std::vector<float> rec((size_t)c.nx * c.nz);
+            for (int ix = 0; ix < c.nx; ix++)
+                std::copy(&st[(size_t)(ix + c.pml) * c.nzz + c.pml], &st[(size_t)(ix + c.pml) * c.nzz + c.pml + c.nz],
+                          &rec[(size_t)ix * c.nz]);
+            wr.append(snap, std::move(rec));
+        }
+        t0 += n;
+    }
+    qpstd_shot_destroy(h);
+    return rc;
+}
+
 // Modeling: gather to "../obsdata/<prefix><shotid>_<nr>.bin"; with flagout the
 // interior p of every tenth step appended to "../obsdata/<snap><shotid>_<nz>_<nx>.bin"
 // (sgpstd-qmodeling/acps4.cu:568-640).
 inline void model(const Common &c, MultiGPU *singpu, int nshot, float *const *models, int kind, int flagout,
                   const char *recpre, const char *snappre) {
     const float fd = cpml_fd(c);
+    AsyncWriter wr;
     for (int ns = 0; ns < nshot; ns++) {
         Shot s;
         if (!window(c, singpu, ns, models, s)) continue;
         qpstd_shot_desc d = describe(c, s, kind, fd);
         std::vector<float> gather((size_t)c.tmax * std::max(s.nr, 1), 0.f);
-        int rc = QPSTD_OK;
-        if (!flagout) {
-            rc = qpstd_model_shot(&d, gather.data(), nullptr);
-        } else {
-            char snap[128];
-            snprintf(snap, sizeof snap, "../obsdata/%s%d_%d_%d.bin", snappre, s.shotid, c.nz, c.nx);
-            FILE *fs = fopen(snap, "wb");
-            if (fs) fclose(fs);
-            qpstd_shot *h = nullptr;
-            rc = qpstd_shot_create(&d, &h);
-            std::vector<float> st((size_t)8 * c.nxx * c.nzz);
-            // steps [0], [1..10], [11..20], ...: the state after every t % 10 == 0
-            for (int t0 = 0; !rc && t0 < c.tmax;) {
-                const int n = (t0 == 0) ? 1 : std::min(10, c.tmax - t0);
-                rc = qpstd_shot_advance(h, t0, n, gather.data() + (size_t)t0 * s.nr);
-                const int tl = t0 + n - 1;
-                if (!rc && tl % 10 == 0 && !(rc = qpstd_shot_get_state(h, st.data()))) {
-                    fs = fopen(snap, "ab");
-                    for (int ix = c.pml; fs && ix < c.nxx - c.pml; ix++)
-                        fwrite(&st[(size_t)ix * c.nzz + c.pml], sizeof(float), c.nzz - 2 * c.pml, fs);
-                    if (fs) fclose(fs);
-                }
-                t0 += n;
-            }
-            qpstd_shot_destroy(h);
-        }
+        const int rc = flagout ? model_with_snapshots(c, s, d, gather.data(), snappre, wr)
+                               : qpstd_model_shot(&d, gather.data(), nullptr);
         report(rc, s.shotid);
-        char name[128];
-        snprintf(name, sizeof name, "../obsdata/%s%d_%d.bin", recpre, s.shotid, s.nr);
-        FILE *fr = fopen(name, "wb");
-        if (fr) {
-            fwrite(gather.data(), sizeof(float), (size_t)c.tmax * s.nr, fr);
-            fclose(fr);
-        }
+        write_gather(c, s, gather.data(), recpre);
     }
 }
 
@@ -205,44 +271,68 @@ inline void model(const Common &c, MultiGPU *singpu, int nshot, float *const *mo
 // removed, the image filtered, muted outside the receiver aperture, projected
 // onto the model and summed into img_sp / ssg_sp (sgpstd-qrtm/acsglw.cu:409-420,
 // 1041-1079).
+// RTM parameters beyond the common ones.
+struct RtmArgs {
+    int kind, snapnum;
+    float fobs, v0, etas, etar;
+    const char *recname;
+};
+
+// One RTM shot made ready: window, observed data with the direct wave removed
+// (obs, nt x nr) and the shot descriptor (pointing into s).
+inline bool rtm_prepare(const Common &c, MultiGPU *singpu, int ns, float *const *models, const RtmArgs &a, Shot &s,
+                        std::vector<float> &obs, qpstd_shot_desc &d) {
+    if (!window(c, singpu, ns, models, s)) return false;
+    obs.assign((size_t)c.tmax * std::max(s.nr, 1), 0.f);
+    char name[256];
+    snprintf(name, sizeof name, "%s%d_%d.bin", a.recname, s.shotid, s.nr);
+    FILE *fr = fopen(name, "rb");
+    if (!fr || fread(obs.data(), sizeof(float), (size_t)c.tmax * s.nr, fr) != (size_t)c.tmax * s.nr)
+        printf("shot %d: cannot read %s\n", s.shotid, name);
+    if (fr) fclose(fr);
+    removedirect(c.nrmx, c.tmax, s.nr, c.dt, a.fobs, s.xs, s.zs, c.gxp, c.gzp, a.v0, obs.data());
+    d = describe(c, s, a.kind, cpml_fd(c));
+    d.snaps = a.snapnum;
+    d.etas = a.etas;
+    d.etar = a.etar;
+    if (a.kind == QPSTD_QRTM) d.taoc = get_max_tao(c.nxx, c.nzz, s.f[7].data());  // acsglw.cu:354-356
+    return true;
+}
+
+// One shot's image (nx x nz) filtered, muted outside the receiver aperture and
+// projected onto the model, summed with its illumination into img_sp / ssg_sp.
+inline int rtm_accumulate(const Common &c, const Shot &s, const float *img, const float *ssg, float *img_sp,
+                          float *ssg_sp) {
+    const size_t NI = (size_t)c.nx * c.nz, NT = (size_t)c.nxt * c.nzt;
+    std::vector<float> imgf(NI), ssgw(ssg, ssg + NI), img_pj(NT, 0.f), ssg_pj(NT, 0.f);
+    const int rc = qpstd_filter_image(c.nx, c.nz, c.dx, c.dz, img, imgf.data());
+    if (rc) return rc;
+    const int lg = s.lgest - c.pml, rg = s.rgest - c.pml;
+    for (int j = 0; j < c.nz; j++) {
+        for (int i = 0; i < lg; i++) imgf[(size_t)i * c.nz + j] = 0.f;
+        for (int i = std::max(rg, 0); i < c.nx; i++) imgf[(size_t)i * c.nz + j] = 0.f;
+    }
+    projectomodel(c.pml, s.mlx, c.dx, c.nxt, c.nzt, c.nx, c.nz, c.nxx, c.nzz, img_pj.data(), imgf.data());
+    projectomodel(c.pml, s.mlx, c.dx, c.nxt, c.nzt, c.nx, c.nz, c.nxx, c.nzz, ssg_pj.data(), ssgw.data());
+    for (size_t i = 0; i < NT; i++) {
+        img_sp[i] += img_pj[i];
+        ssg_sp[i] += ssg_pj[i];
+    }
+    return QPSTD_OK;
+}
+
 inline void rtm(const Common &c, MultiGPU *singpu, int nshot, float *const *models, int kind, int snapnum,
                 float *img_sp, float *ssg_sp, float fobs, float v0, float etas, float etar, const char *recname) {
-    const float fd = cpml_fd(c);
-    const size_t NI = (size_t)c.nx * c.nz, NT = (size_t)c.nxt * c.nzt;
-    std::vector<float> img(NI), imgf(NI), ssg(NI), img_pj(NT), ssg_pj(NT);
+    const RtmArgs a{kind, snapnum, fobs, v0, etas, etar, recname};
+    const size_t NI = (size_t)c.nx * c.nz;
+    std::vector<float> img(NI), ssg(NI), obs;
     for (int ns = 0; ns < nshot; ns++) {
         Shot s;
-        if (!window(c, singpu, ns, models, s)) continue;
-        std::vector<float> obs((size_t)c.tmax * std::max(s.nr, 1), 0.f);
-        char name[256];
-        snprintf(name, sizeof name, "%s%d_%d.bin", recname, s.shotid, s.nr);
-        FILE *fr = fopen(name, "rb");
-        if (!fr || fread(obs.data(), sizeof(float), (size_t)c.tmax * s.nr, fr) != (size_t)c.tmax * s.nr)
-            printf("shot %d: cannot read %s\n", s.shotid, name);
-        if (fr) fclose(fr);
-        removedirect(c.nrmx, c.tmax, s.nr, c.dt, fobs, s.xs, s.zs, c.gxp, c.gzp, v0, obs.data());
-        qpstd_shot_desc d = describe(c, s, kind, fd);
-        d.snaps = snapnum;
-        d.etas = etas;
-        d.etar = etar;
-        if (kind == QPSTD_QRTM) d.taoc = get_max_tao(c.nxx, c.nzz, s.f[7].data());  // acsglw.cu:354-356
+        qpstd_shot_desc d;
+        if (!rtm_prepare(c, singpu, ns, models, a, s, obs, d)) continue;
         int rc = qpstd_rtm_shot(&d, obs.data(), img.data(), ssg.data());
-        if (!rc) rc = qpstd_filter_image(c.nx, c.nz, c.dx, c.dz, img.data(), imgf.data());
+        if (!rc) rc = rtm_accumulate(c, s, img.data(), ssg.data(), img_sp, ssg_sp);
         report(rc, s.shotid);
-        if (rc) continue;
-        const int lg = s.lgest - c.pml, rg = s.rgest - c.pml;
-        for (int j = 0; j < c.nz; j++) {
-            for (int i = 0; i < lg; i++) imgf[(size_t)i * c.nz + j] = 0.f;
-            for (int i = std::max(rg, 0); i < c.nx; i++) imgf[(size_t)i * c.nz + j] = 0.f;
-        }
-        std::fill(img_pj.begin(), img_pj.end(), 0.f);
-        std::fill(ssg_pj.begin(), ssg_pj.end(), 0.f);
-        projectomodel(c.pml, s.mlx, c.dx, c.nxt, c.nzt, c.nx, c.nz, c.nxx, c.nzz, img_pj.data(), imgf.data());
-        projectomodel(c.pml, s.mlx, c.dx, c.nxt, c.nzt, c.nx, c.nz, c.nxx, c.nzz, ssg_pj.data(), ssg.data());
-        for (size_t i = 0; i < NT; i++) {
-            img_sp[i] += img_pj[i];
-            ssg_sp[i] += ssg_pj[i];
-        }
     }
 }
 

@@ -43,6 +43,102 @@ def pf(a):
     return a.ctypes.data_as(fp)
 
 
+# Parameter files of the four programs: (reference library, file name, fields),
+# each field (kind, value) with kind i / f / s; values are synthetic.
+PARAM_FILES = {
+    "aps": ("qm_funca", "ac2drealmodeling.txt",
+            [("i", 7), ("i", 1201), ("f", 0.75), ("f", 22.5), ("i", 301), ("i", 97), ("f", 12.5), ("f", 10.0),
+             ("f", 35.0), ("s", "../g/tn.bin"), ("s", "../g/sx.bin"), ("s", "../g/sz.bin"), ("s", "../g/gx"),
+             ("s", "../g/gz"), ("s", "../m/vp.bin"), ("s", "../m/rho.bin"), ("i", 1), ("i", 1)]),
+    "vaps": ("qm_func", "visac2drealmodeling.txt",
+             [("i", 9), ("i", 1500), ("f", 0.5), ("f", 25.0), ("f", 150.0), ("i", 256), ("i", 120), ("f", 10.0),
+              ("f", 7.5), ("f", 0.0), ("s", "../g/tn.bin"), ("s", "../g/sx.bin"), ("s", "../g/sz.bin"),
+              ("s", "../g/gx"), ("s", "../g/gz"), ("s", "../m/vp.bin"), ("s", "../m/rho.bin"),
+              ("s", "../m/qp.bin"), ("i", 0), ("i", 2)]),
+    "artm": ("qr_funca", "ac2drtm.txt",
+             [("i", 12), ("i", 3001), ("f", 0.5), ("f", 18.0), ("i", 800), ("i", 240), ("f", 10.0), ("f", 10.0),
+              ("f", 100.0), ("f", 1480.0), ("s", "../g/tn.bin"), ("s", "../g/sx.bin"), ("s", "../g/sz.bin"),
+              ("s", "../g/gx"), ("s", "../g/gz"), ("s", "../m/vpm.bin"), ("s", "../m/rho.bin"),
+              ("s", "../obs/reca"), ("i", 2), ("i", 25)]),
+    "qrtm": ("qr_func", "visac2drtm.txt",
+             [("i", 64), ("i", 5000), ("f", 0.5), ("f", 30.0), ("f", 200.0), ("i", 6000), ("i", 600),
+              ("f", 10.0), ("f", 10.0), ("f", 0.0), ("f", 1500.0), ("f", 1e-20), ("f", 3e-20),
+              ("s", "../g/tn.bin"), ("s", "../g/sx.bin"), ("s", "../g/sz.bin"), ("s", "../g/gx"), ("s", "../g/gz"),
+              ("s", "../m/vpm.bin"), ("s", "../m/rho.bin"), ("s", "../m/qp.bin"), ("s", "../obs/recva"),
+              ("i", 2), ("i", 30)]),
+}
+# geometry/parameters.txt variants: shotnum, sx0, sxdx, sdep, rdep, offset, trdx, dx, dz, nx, nz
+GEOMETRY = [
+    (6, 400.0, 40.0, 0.0, 0.0, 1500.0, 10.0, 10.0, 10.0, 398, 160),
+    (5, 15.0, 237.5, 20.0, 12.5, 333.3, 7.5, 12.5, 12.5, 97, 41),
+]
+
+
+def param_text(fields):
+    """Label lines and values, with blank lines and trailing blanks the readers skip."""
+    lines = []
+    for k, (kind, v) in enumerate(fields):
+        lines.append(f"--field {k} ({kind})")
+        if k % 3 == 1:
+            lines.append("")
+        lines.append(f"  {v!r}" if kind == "f" else f"  {v}" + ("  " if k % 2 else ""))
+    return "\n".join(lines) + "\n"
+
+
+def program_fixtures(out):
+    """The programs' own parameter readers and geometry generator on synthetic files."""
+    import subprocess
+    import tempfile
+
+    cwd = os.getcwd()
+    for prog, (libname, fname, fields) in PARAM_FILES.items():
+        lib = O.ref_lib(libname)
+        d = tempfile.mkdtemp(prefix="qpar")
+        os.makedirs(os.path.join(d, "input"))
+        os.makedirs(os.path.join(d, "run"))
+        text = param_text(fields)
+        with open(os.path.join(d, "input", fname), "w") as f:
+            f.write(text)
+        args, back = [], []
+        for k, (kind, _) in enumerate(fields):
+            if kind == "i":
+                a = C.c_int(0)
+                args.append(C.byref(a))
+            elif kind == "f":
+                a = C.c_float(0.0)
+                args.append(C.byref(a))
+            else:
+                a = C.create_string_buffer(128)
+                args.append(a)
+            back.append((kind, a))
+        os.chdir(os.path.join(d, "run"))
+        try:
+            lib.input_ac2d_parameters(*args)
+        finally:
+            os.chdir(cwd)
+        nums = [float(a.value) for kind, a in back if kind != "s"]
+        strs = "\n".join(a.value.decode() for kind, a in back if kind == "s")
+        out[f"par_{prog}_text"] = np.frombuffer(text.encode(), dtype=np.uint8)
+        out[f"par_{prog}_nums"] = np.array(nums, dtype=np.float64)
+        out[f"par_{prog}_strs"] = np.frombuffer(strs.encode(), dtype=np.uint8)
+    exe = os.path.join(HERE, "..", "..", "oracle", "_ref", "geometry2d")
+    for gi, g in enumerate(GEOMETRY):
+        d = tempfile.mkdtemp(prefix="qgeo")
+        labels = ["shots", "first x", "interval", "shot depth", "receiver depth", "offset", "trace interval",
+                  "dx", "dz", "nx", "nz"]
+        with open(os.path.join(d, "parameters.txt"), "w") as f:
+            for lab, v in zip(labels, g):
+                f.write(f"-- {lab}\n   {v}\n")
+        subprocess.run([os.path.abspath(exe)], cwd=d, check=True, capture_output=True)
+        rd = lambda n, t: np.fromfile(os.path.join(d, n), dtype=t)
+        out[f"geo{gi}_params"] = np.array(g, dtype=np.float64)
+        out[f"geo{gi}_tracenum"] = rd("tracenum.bin", np.int32)
+        out[f"geo{gi}_shotxp"] = rd("shotxp.bin", np.float32)
+        out[f"geo{gi}_shotzp"] = rd("shotzp.bin", np.float32)
+        out[f"geo{gi}_gxp"] = np.concatenate([rd(f"gxp{i}.bin", np.float32) for i in range(g[0])])
+        out[f"geo{gi}_gzp"] = np.concatenate([rd(f"gzp{i}.bin", np.float32) for i in range(g[0])])
+
+
 def main():
     qm_a = O.ref_lib("qm_funca")
     qm_f = O.ref_lib("qm_func")
@@ -134,6 +230,7 @@ def main():
             if a in (5, 6):
                 break
         out[f"revolve_{steps}_{snaps}"] = np.array(tr, dtype=np.int32)
+    program_fixtures(out)
     path = os.path.join(HERE, "reference_host.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, os.path.getsize(path), "bytes")
