@@ -120,8 +120,10 @@ __global__ void __launch_bounds__(768, 1) ac_zpass_kernel(AcZArgs a) {
 }
 
 // ---- x pass ----------------------------------------------------------------
-// staged fields (each nxx*2L floats, in the (ix, c) walk order):
-//   0 div, 1 Lz, 2 p, 3 c1, 4 c2, 5 psi_px, 6 vx, 7 bbx, 8 psi_vx
+// Staged fields (xstage_fields; each nxx*2L floats, in the (ix, c) walk order,
+// only the fields of the pass's mode).  Without the p update, the input of the
+// first transform (p, or vx) is its own cp.async group, so the transform starts
+// while the epilogue inputs are still arriving.
 __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
@@ -131,8 +133,20 @@ __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
     float* sf = reinterpret_cast<float*>(smem);
     float* stg = reinterpret_cast<float*>(smem + (size_t)L * ld);
     const size_t fstride = (size_t)T.tot;
-    auto S = [&](int f, int g) -> float& { return stg[f * fstride + g]; };
+    const unsigned fm = xstage_fields(a.do_p, a.do_v, a.do_dx);
+    auto S = [&](int f, int g) -> float& { return stg[__popc(fm & ((1u << f) - 1u)) * fstride + g]; };
     if (a.stage) {
+        const float* first = a.do_v ? a.p : a.vx;  // the first transform's input when !do_p
+        const int ff = a.do_v ? 2 : 6;
+        if (!a.do_p) {
+            for (int g = T.t0; g < T.tot; g += T.nthr) {
+                int c, ix;
+                T.split(g, c, ix);
+                const int iz = T.iz0 + c;
+                if (iz < nzz) cp_async4(&S(ff, g), first + (size_t)ix * nzz + iz);
+            }
+            cp_async_commit();
+        }
         for (int g = T.t0; g < T.tot; g += T.nthr) {
             int c, ix;
             T.split(g, c, ix);
@@ -144,16 +158,12 @@ __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
                 cp_async4(&S(2, g), a.p + i);
                 cp_async4(&S(3, g), a.c1 + i);
                 cp_async4(&S(4, g), a.c2 + i);
-            } else if (a.do_v) {
-                cp_async4(&S(2, g), a.p + i);
             }
             if (a.do_v) {
                 cp_async4(&S(5, g), a.psi_px + i);
-                cp_async4(&S(6, g), a.vx + i);
                 cp_async4(&S(7, g), a.bbx + i);
-            } else if (a.do_dx) {
-                cp_async4(&S(6, g), a.vx + i);
             }
+            if ((a.do_v || a.do_dx) && (a.do_p || ff != 6)) cp_async4(&S(6, g), a.vx + i);
             if (a.do_dx) cp_async4(&S(8, g), a.psi_vx + i);
         }
         cp_async_commit();
@@ -222,7 +232,7 @@ __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
     }
     if (a.do_v) {
         if (!have) {
-            if (a.stage) cp_async_wait_all();
+            if (a.stage) cp_async_wait_prior();  // p (first group) has landed
             for (int g = T.t0; g < T.tot; g += T.nthr) {
                 int c, ix;
                 T.split(g, c, ix);
@@ -257,7 +267,11 @@ __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
     }
     if (a.do_dx) {
         if (!have) {
-            if (a.stage) cp_async_wait_all();
+            // vx: the first group without the p update, else in the only group
+            if (a.stage) {
+                if (a.do_p) cp_async_wait_all();
+                else cp_async_wait_prior();
+            }
             for (int g = T.t0; g < T.tot; g += T.nthr) {
                 int c, ix;
                 T.split(g, c, ix);
@@ -286,8 +300,8 @@ __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
 size_t ac_zpass_smem(int L, int m, int nzz, bool stage) {
     return sizeof(float2) * (size_t)L * m + (stage ? sizeof(float) * 5 * (size_t)L * 2 * nzz : 0);
 }
-size_t ac_xpass_smem(int L, int m, int nxx, bool stage) {
-    return sizeof(float2) * (size_t)L * m + (stage ? sizeof(float) * 9 * (size_t)nxx * 2 * L : 0);
+size_t ac_xpass_smem(int L, int m, int nxx, int nstaged) {
+    return sizeof(float2) * (size_t)L * m + sizeof(float) * (size_t)nstaged * nxx * 2 * L;
 }
 
 void launch_ac_zpass(const AcZArgs& a, cudaStream_t s) {
@@ -297,7 +311,8 @@ void launch_ac_zpass(const AcZArgs& a, cudaStream_t s) {
 
 void launch_ac_xpass(const AcXArgs& a, cudaStream_t s) {
     const int grid = (a.nzz + 2 * a.L - 1) / (2 * a.L);
-    ac_xpass_kernel<<<grid, dim3(a.pl.tx, a.L), ac_xpass_smem(a.L, a.pl.m, a.nxx, a.stage), s>>>(a);
+    const int nst = a.stage ? xstage_count(xstage_fields(a.do_p, a.do_v, a.do_dx)) : 0;
+    ac_xpass_kernel<<<grid, dim3(a.pl.tx, a.L), ac_xpass_smem(a.L, a.pl.m, a.nxx, nst), s>>>(a);
 }
 
 int ac_set_smem_limits() {

@@ -16,6 +16,8 @@ __device__ __forceinline__ void cp_async4(float* sdst, const float* gsrc) {
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+// Waits for every committed group but the most recent one.
+__device__ __forceinline__ void cp_async_wait_prior() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
 // Compensated accumulation s += v (Kahan), used for the image and the
 // illumination sums over thousands of steps.

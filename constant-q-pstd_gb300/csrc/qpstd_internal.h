@@ -71,6 +71,22 @@ struct AcZArgs {
 //   do_v : Px = dx+ p; psi_px; vx += dt bbx (Px + psi_px)
 //   do_dx: Dx = dx- vx + psi_vx (psi_vx updated)
 // ---------------------------------------------------------------------------
+// Fields the x pass stages in shared memory for its mode (bit f = field f):
+// 0 div, 1 Lz, 2 p, 3 c1, 4 c2, 5 psi_px, 6 vx, 7 bbx, 8 psi_vx.  Each staged
+// field takes nxx * 2L floats, in slot order (the rank of its bit).
+__host__ __device__ inline unsigned xstage_fields(int do_p, int do_v, int do_dx) {
+    unsigned m = 0;
+    if (do_p) m |= 0x1Fu;
+    if (do_v) m |= (1u << 2) | (1u << 5) | (1u << 6) | (1u << 7);
+    if (do_dx) m |= (1u << 6) | (1u << 8);
+    return m;
+}
+__host__ __device__ inline int xstage_count(unsigned m) {
+    int n = 0;
+    for (; m; m &= m - 1) n++;
+    return n;
+}
+
 struct AcXArgs {
     int nxx, nzz, L, pml;
     FFTPlanDev pl;                // convolution plan along x
@@ -130,7 +146,7 @@ struct VxsArgs {
     const float *kx2, *kz2;   // squared wavenumbers (unnormalised)
     const float2* in;
     float2 *out0, *out1, *out2;
-    const float *tab0, *tab1, *tab2;  // per-kz convolution multipliers, nzh x plc.m (modes 0, 1)
+    const float *tab0, *tab1, *tab2;  // per-kz convolution multipliers, nzh x (plc.m/2+1) (modes 0, 1)
     float norm;               // 1/(nxx*nzz)
     float eta6;               // eta * 1e-6 (mode 2)
     float tao, dt, tt;        // filter tau, dt, nt*dt (mode 2)
@@ -138,7 +154,8 @@ struct VxsArgs {
 
 // Builds the per-kz convolution multipliers of a stationary 2-D symbol:
 // for each kz, h = norm * IDFT_x(sym(kx, kz)) zero-padded and wrapped to
-// plc.m, then out[kz*plc.m + k] = Re FFT_m(h)[k] / m.
+// plc.m, then out[kz*mh + k] = Re FFT_m(h)[k] / m for k = 0..m/2, mh = m/2+1
+// (h is real and even, so the multipliers are real and even in k).
 struct VtabArgs {
     int nxx, nzz, nzh, L, sym;  // sym: 0 (k^2)^(1/32), 1 k^2, 2 (k^2)^(33/32), 3 (k^2)^0.505
     FFTPlanDev pl, plc;

@@ -173,10 +173,12 @@ __global__ void __launch_bounds__(768, 1) vz_xspec_conv_kernel(VxsArgs a) {
         for (int k = threadIdx.x; k < m; k += blockDim.x) X[threadIdx.y * ld + k] = line[k];
         __syncthreads();
     }
+    // the multipliers are even in k: rows hold entries 0..m/2
+    const int mh = m / 2 + 1;
     auto output = [&](const float* __restrict__ tab, float2* out) {
         const float2* src = (nout == 3) ? X + threadIdx.y * ld : line;
-        const float* tk = tab + (size_t)kz * m;
-        for (int k = threadIdx.x; k < m; k += blockDim.x) line[k] = cscale(src[k], __ldg(&tk[k]));
+        const float* tk = tab + (size_t)kz * mh;
+        for (int k = threadIdx.x; k < m; k += blockDim.x) line[k] = cscale(src[k], __ldg(&tk[min(k, m - k)]));
         __syncthreads();
         fft_m<+1>(smem, ld, fc, L);
         for (int g = t0; g < tot; g += nthr) {
@@ -225,8 +227,10 @@ __global__ void __launch_bounds__(768, 1) vz_convtab_kernel(VtabArgs a) {
     for (int k = threadIdx.x; k < m; k += blockDim.x) line[k] = make_float2(line[k].x * a.norm, 0.f);
     __syncthreads();
     fft_m<-1>(smem, ld, fcc, L);
+    // the wrapped kernel is even, so its transform is real and even: keep 0..m/2
+    const int mh = m / 2 + 1;
     if (valid)
-        for (int k = threadIdx.x; k < m; k += blockDim.x) a.out[(size_t)kz * m + k] = line[k].x / (float)m;
+        for (int k = threadIdx.x; k < mh; k += blockDim.x) a.out[(size_t)kz * mh + k] = line[k].x / (float)m;
 }
 
 // ---- z pass B -----------------------------------------------------------------
