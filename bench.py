@@ -88,6 +88,14 @@ def workload(name: str):
         desc = {"workload": "artm3", "kind": "artm", "shots": 1, "grid": [d["nxx"], d["nzz"]], "nt": 6000,
                 "snaps": 40, "receivers": int(len(d["gxg"])), "obs": "fused aps modeling on the unsmoothed model"}
         return [d], "artm", seed, desc, lambda dd, i: qpstd.model_shot(true)
+    if name == "vaps2":
+        seed = 1002
+        d = W.make_shot(qpstd.VAPS, 398, 160, 20, 3000, 0.001, 20.0, seed=seed, nlayers=5, nanom=1, fo=20.0)
+        desc = {"workload": "vaps2", "kind": "vaps", "shots": 1, "grid": [d["nxx"], d["nzz"]], "nt": 3000,
+                "fo": 20.0, "q": "per layer U(20, 200)",
+                "form": "power-expansion (executed reference form); the rank-4 low-rank operator is timed "
+                        "on the same window under 'lowrank'"}
+        return [d], "vaps", seed, desc, None
     if name == "aps1":
         seed = 1001
         d = W.make_shot(0, 398, 160, 20, 2000, 0.001, 20.0, seed=seed, nlayers=5, nanom=1)
@@ -219,6 +227,37 @@ def cpu_baseline(shots, kname: str, budget_s: float):
     rate, el = oracle_rate(d, kname, n)
     return {"value": rate, "unit": "Gpts/s", "cores": os.cpu_count(), "kind": "port",
             "sample": f"{n} FP64 oracle time steps of shot 0 ({d['nxx']}x{d['nzz']}), {el:.1f} s"}
+
+
+def time_lowrank(d: dict, rank: int, reps: int = 50):
+    """The low-rank form of the constant-Q symbol (sgpstd-qmodeling/sglowrank.c) on the
+    shot's window: host FP64 decomposition, then device applications timed with CUDA
+    events on the operator's stream (input and output resident in HBM)."""
+    import torch
+
+    import qpstd
+
+    nxx, nzz = d["nxx"], d["nzz"]
+    t0 = time.perf_counter()
+    f = qpstd.lowrank_decompose(nxx, nzz, d["dx"], d["dz"], d["dt"], d["vp"], d["tao"], d["gam"], rank, rank)
+    t_dec = time.perf_counter() - t0
+    op = qpstd.LowRank(f)
+    x = torch.randn(nxx * nzz, device="cuda")
+    y = torch.empty_like(x)
+    s = torch.cuda.Stream()
+    for _ in range(5):
+        op.apply_device(x.data_ptr(), y.data_ptr(), s.cuda_stream)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(s)
+    for _ in range(reps):
+        op.apply_device(x.data_ptr(), y.data_ptr(), s.cuda_stream)
+    b.record(s)
+    torch.cuda.synchronize()
+    us = a.elapsed_time(b) * 1000.0 / reps
+    op.close()
+    return {"rank": rank, "grid": [nxx, nzz], "us_per_apply": us, "gpts_per_s": nxx * nzz / us / 1e3,
+            "decompose_s": t_dec, "note": "one application of sum_a U[x,a] sum_b A[a,b] Re F^-1[V_b F p] / N"}
 
 
 def run_reference(args, ws, rank):
@@ -487,6 +526,8 @@ def main():
     }
     del B
     torch.cuda.synchronize()
+    if args.workload == "vaps2":
+        out["lowrank"] = time_lowrank(shots[0], rank=4)
     # ---- per-shot plain cuFFT path on the same GPU (the baseline of the batching claim)
     if not args.no_plain:
         d0 = shots[0]

@@ -392,6 +392,10 @@ class LowRank:
         _check(lib().qpstd_lowrank_apply(self.h, _f(a), _f(out)))
         return out
 
+    def apply_device(self, d_in: int, d_out: int, stream: int = 0) -> None:
+        """Device pointers (nxx*nzz float32 each), enqueued on the given CUDA stream."""
+        _check(lib().qpstd_lowrank_apply_device(self.h, C.c_void_p(d_in), C.c_void_p(d_out), C.c_void_p(stream)))
+
     def close(self):
         if self.h:
             lib().qpstd_lowrank_destroy(self.h)
