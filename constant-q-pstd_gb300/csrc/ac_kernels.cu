@@ -124,6 +124,7 @@ __global__ void __launch_bounds__(768, 1) ac_zpass_kernel(AcZArgs a) {
 // only the fields of the pass's mode).  Without the p update, the input of the
 // first transform (p, or vx) is its own cp.async group, so the transform starts
 // while the epilogue inputs are still arriving.
+template <bool P>  // P: this launch does the p update (a.do_p)
 __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
@@ -133,12 +134,12 @@ __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
     float* sf = reinterpret_cast<float*>(smem);
     float* stg = reinterpret_cast<float*>(smem + (size_t)L * ld);
     const size_t fstride = (size_t)T.tot;
-    const unsigned fm = xstage_fields(a.do_p, a.do_v, a.do_dx);
+    const unsigned fm = xstage_fields(P, a.do_v, a.do_dx);
     auto S = [&](int f, int g) -> float& { return stg[__popc(fm & ((1u << f) - 1u)) * fstride + g]; };
     if (a.stage) {
         const float* first = a.do_v ? a.p : a.vx;  // the first transform's input when !do_p
         const int ff = a.do_v ? 2 : 6;
-        if (!a.do_p) {
+        if (!P) {
             for (int g = T.t0; g < T.tot; g += T.nthr) {
                 int c, ix;
                 T.split(g, c, ix);
@@ -153,7 +154,7 @@ __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
             const int iz = T.iz0 + c;
             if (iz >= nzz) continue;
             const size_t i = (size_t)ix * nzz + iz;
-            if (a.do_p) {
+            if (P) {
                 cp_async4(&S(1, g), a.Lz + i);
                 cp_async4(&S(2, g), a.p + i);
                 cp_async4(&S(3, g), a.c1 + i);
@@ -163,14 +164,14 @@ __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
                 cp_async4(&S(5, g), a.psi_px + i);
                 cp_async4(&S(7, g), a.bbx + i);
             }
-            if ((a.do_v || a.do_dx) && (a.do_p || ff != 6)) cp_async4(&S(6, g), a.vx + i);
+            if ((a.do_v || a.do_dx) && (P || ff != 6)) cp_async4(&S(6, g), a.vx + i);
             if (a.do_dx) cp_async4(&S(8, g), a.psi_vx + i);
         }
         cp_async_commit();
     }
 
     bool have = false;  // smem holds the packed field for the next transform
-    if (a.do_p) {
+    if (P) {
         // div feeds the first transform now and the p update later
         for (int g = T.t0; g < T.tot; g += T.nthr) {
             int c, ix;
@@ -269,7 +270,7 @@ __global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
         if (!have) {
             // vx: the first group without the p update, else in the only group
             if (a.stage) {
-                if (a.do_p) cp_async_wait_all();
+                if (P) cp_async_wait_all();
                 else cp_async_wait_prior();
             }
             for (int g = T.t0; g < T.tot; g += T.nthr) {
@@ -312,14 +313,18 @@ void launch_ac_zpass(const AcZArgs& a, cudaStream_t s) {
 void launch_ac_xpass(const AcXArgs& a, cudaStream_t s) {
     const int grid = (a.nzz + 2 * a.L - 1) / (2 * a.L);
     const int nst = a.stage ? xstage_count(xstage_fields(a.do_p, a.do_v, a.do_dx)) : 0;
-    ac_xpass_kernel<<<grid, dim3(a.pl.tx, a.L), ac_xpass_smem(a.L, a.pl.m, a.nxx, nst), s>>>(a);
+    const size_t sm = ac_xpass_smem(a.L, a.pl.m, a.nxx, nst);
+    // the instance without the p update carries only the transforms it runs
+    if (a.do_p) ac_xpass_kernel<true><<<grid, dim3(a.pl.tx, a.L), sm, s>>>(a);
+    else ac_xpass_kernel<false><<<grid, dim3(a.pl.tx, a.L), sm, s>>>(a);
 }
 
 int ac_set_smem_limits() {
     const int lim = QP_SMEM_DYN_MAX;
     cudaError_t e1 = cudaFuncSetAttribute(ac_zpass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-    cudaError_t e2 = cudaFuncSetAttribute(ac_xpass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-    return (e1 == cudaSuccess && e2 == cudaSuccess) ? 0 : -1;
+    cudaError_t e2 = cudaFuncSetAttribute(ac_xpass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaError_t e3 = cudaFuncSetAttribute(ac_xpass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    return (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess) ? 0 : -1;
 }
 
 }  // namespace qp

@@ -148,6 +148,8 @@ __global__ void __launch_bounds__(768, 1) vz_xspec_kernel(VxsArgs a) {
 // convolution along x, so a zero-padded FFT on the smooth convolution length
 // replaces the exact (Bluestein) DFTs: one forward transform, then per output a
 // multiply by the column's table and one inverse transform.
+// NOUT = 3 (mode 0) or 1 (mode 1): each instance carries only the transforms it runs.
+template <int NOUT>
 __global__ void __launch_bounds__(768, 1) vz_xspec_conv_kernel(VxsArgs a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
@@ -157,7 +159,7 @@ __global__ void __launch_bounds__(768, 1) vz_xspec_conv_kernel(VxsArgs a) {
     const int kz0 = blockIdx.x * L;
     const int t0 = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
     const int tot = L * nxx;
-    const int nout = (a.mode == 0) ? 3 : 1;
+    constexpr int nout = NOUT;
     float2* X = smem + (size_t)L * ld;  // kept forward spectrum (three-output mode)
     float2* line = smem + threadIdx.y * ld;
     for (int g = t0; g < tot; g += nthr) {
@@ -377,7 +379,9 @@ void launch_vz_xspec(const VxsArgs& a, cudaStream_t s) {
     vz_xspec_kernel<<<(a.nzh + a.L - 1) / a.L, dim3(a.pl.tx, a.L), lsm(a.L, a.pl.m, a.mode == 0 ? 2 : 1), s>>>(a);
 }
 void launch_vz_xspec_conv(const VxsArgs& a, cudaStream_t s) {
-    vz_xspec_conv_kernel<<<(a.nzh + a.L - 1) / a.L, dim3(a.plc.tx, a.L), lsm(a.L, a.plc.m, a.mode == 0 ? 2 : 1), s>>>(a);
+    const int grid = (a.nzh + a.L - 1) / a.L;
+    if (a.mode == 0) vz_xspec_conv_kernel<3><<<grid, dim3(a.plc.tx, a.L), lsm(a.L, a.plc.m, 2), s>>>(a);
+    else vz_xspec_conv_kernel<1><<<grid, dim3(a.plc.tx, a.L), lsm(a.L, a.plc.m, 1), s>>>(a);
 }
 void launch_vz_convtab(const VtabArgs& a, cudaStream_t s) {
     vz_convtab_kernel<<<(a.nzh + a.L - 1) / a.L, dim3(max(a.pl.tx, a.plc.tx), a.L), lsm(a.L, max(a.pl.m, a.plc.m), 1), s>>>(a);
@@ -396,7 +400,8 @@ int vz_set_smem_limits() {
     int bad = 0;
     bad |= cudaFuncSetAttribute(vz_passA_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_xspec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_convtab_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_passB_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_passC_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
