@@ -323,6 +323,9 @@ void usage() {
 }  // namespace
 
 int main(int argc, char **argv) {
+    // shots run on one stream each: 32 hardware work queues (the default is 8);
+    // read when the CUDA context is created, so before any CUDA call
+    setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
     std::string self = argv[0];
     const size_t slash = self.find_last_of('/');
     if (slash != std::string::npos) self = self.substr(slash + 1);
