@@ -23,7 +23,7 @@ namespace qp {
 
 // ---- z pass ----------------------------------------------------------------
 // staged fields (each L*2*nzz floats): 0 vz, 1 psi_pz, 2 bbz, 3 psi_vz, 4 Dx
-__global__ void __launch_bounds__(768, 1) ac_zpass_kernel(AcZArgs a) {
+__global__ void __maxnreg__(QP_PASS_REGS) ac_zpass_kernel(AcZArgs a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
     const FFTCtx fc = make_ctx(a.pl, s_pass);
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(768, 1) ac_zpass_kernel(AcZArgs a) {
 // first transform (p, or vx) is its own cp.async group, so the transform starts
 // while the epilogue inputs are still arriving.
 template <bool P>  // P: this launch does the p update (a.do_p)
-__global__ void __launch_bounds__(768, 1) ac_xpass_kernel(AcXArgs a) {
+__global__ void __maxnreg__(QP_PASS_REGS) ac_xpass_kernel(AcXArgs a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
     const FFTCtx fc = make_ctx(a.pl, s_pass);

@@ -6,6 +6,12 @@
 // Threads per CTA of the pass kernels (__launch_bounds__(QP_MAXTHREADS, 1):
 // 80 registers per thread, enough for the radix-16 butterflies).
 #define QP_MAXTHREADS 768
+// Register cap of the step's pass kernels: at 56 they compile spill-free and hold
+// 4 (not 3) 256-thread line CTAs, or 9 (not 8) 128-thread ones, per SM, which
+// matters when many shots share the GPU.  The three-output x-spectral pass and the
+// exact-DFT x-spectral pass spill at 56 and keep the 80 of the launch bound.
+#define QP_PASS_REGS 56
+#define QP_WIDE_REGS 80
 // Dynamic shared memory a pass kernel may request: the 227 KB per-CTA opt-in
 // minus the static plan copies.
 #define QP_SMEM_DYN_MAX (232448 - 1024)

@@ -34,7 +34,7 @@ namespace qp {
     (void)r1;
 
 // ---- z pass A ---------------------------------------------------------------
-__global__ void __launch_bounds__(768, 1) vz_passA_kernel(VzArgsA a) {
+__global__ void __maxnreg__(QP_PASS_REGS) vz_passA_kernel(VzArgsA a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
     __shared__ FFTPass s_pass_c[QP_MAXST];
@@ -150,7 +150,8 @@ __global__ void __launch_bounds__(768, 1) vz_xspec_kernel(VxsArgs a) {
 // multiply by the column's table and one inverse transform.
 // NOUT = 3 (mode 0) or 1 (mode 1): each instance carries only the transforms it runs.
 template <int NOUT>
-__global__ void __launch_bounds__(768, 1) vz_xspec_conv_kernel(VxsArgs a) {
+__global__ void __maxnreg__(NOUT == 1 ? QP_PASS_REGS : QP_WIDE_REGS)
+    vz_xspec_conv_kernel(VxsArgs a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
     const FFTCtx fc = make_ctx(a.plc, s_pass);
@@ -236,7 +237,7 @@ __global__ void __launch_bounds__(768, 1) vz_convtab_kernel(VtabArgs a) {
 }
 
 // ---- z pass B -----------------------------------------------------------------
-__global__ void __launch_bounds__(768, 1) vz_passB_kernel(VzArgsB a) {
+__global__ void __maxnreg__(QP_PASS_REGS) vz_passB_kernel(VzArgsB a) {
     ZPASS_SETUP
     const int nzh = a.nzh;
     float2* acc = smem + (size_t)(L + threadIdx.y) * ld;  // running total of this line pair
@@ -276,7 +277,7 @@ __global__ void __launch_bounds__(768, 1) vz_passB_kernel(VzArgsB a) {
 }
 
 // ---- z pass C -----------------------------------------------------------------
-__global__ void __launch_bounds__(768, 1) vz_passC_kernel(VzArgsC a) {
+__global__ void __maxnreg__(QP_PASS_REGS) vz_passC_kernel(VzArgsC a) {
     ZPASS_SETUP
     const int nzh = a.nzh;
     zrepack(a.Dspec, line, nzz, nzh, has0, has1, xa);
@@ -356,7 +357,7 @@ __global__ void __launch_bounds__(768, 1) vz_passC_kernel(VzArgsC a) {
 }
 
 // ---- z inverse only -------------------------------------------------------------
-__global__ void __launch_bounds__(768, 1) vz_zinv_kernel(VzArgsI a) {
+__global__ void __maxnreg__(QP_PASS_REGS) vz_zinv_kernel(VzArgsI a) {
     ZPASS_SETUP
     zrepack(a.spec, line, nzz, a.nzh, has0, has1, xa);
     __syncthreads();
