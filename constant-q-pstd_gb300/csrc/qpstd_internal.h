@@ -8,10 +8,14 @@
 #define QP_MAXTHREADS 768
 // Register cap of the step's pass kernels: at 56 they compile spill-free and hold
 // 4 (not 3) 256-thread line CTAs, or 9 (not 8) 128-thread ones, per SM, which
-// matters when many shots share the GPU.  The three-output x-spectral pass and the
-// exact-DFT x-spectral pass spill at 56 and keep the 80 of the launch bound.
+// matters when many shots share the GPU.  The three-output x-spectral pass keeps
+// 80: capped, it measured slower (at 56 without spills, four of its 54 KB CTAs per
+// SM leave too little L1 for its table and twiddle loads).  The exact-DFT
+// x-spectral pass (Bluestein transforms and the Q-RTM filter's exponentials)
+// spills below 72 and takes that cap.
 #define QP_PASS_REGS 56
 #define QP_WIDE_REGS 80
+#define QP_EXACT_REGS 72
 // Dynamic shared memory a pass kernel may request: the 227 KB per-CTA opt-in
 // minus the static plan copies.
 #define QP_SMEM_DYN_MAX (232448 - 1024)

@@ -98,7 +98,7 @@ __device__ __forceinline__ float spec_symbol(const VxsArgs& a, int j, float k2) 
     return ka - num / den;
 }
 
-__global__ void __launch_bounds__(768, 1) vz_xspec_kernel(VxsArgs a) {
+__global__ void __maxnreg__(QP_EXACT_REGS) vz_xspec_kernel(VxsArgs a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
     const FFTCtx fc = make_ctx(a.pl, s_pass);
@@ -117,29 +117,37 @@ __global__ void __launch_bounds__(768, 1) vz_xspec_kernel(VxsArgs a) {
     }
     __syncthreads();
     dft_n<-1>(smem, ld, fc, L);
-    const int kz = kz0 + threadIdx.y;
-    const float kzsq = a.kz2[(kz < nzh) ? kz : 0];
     if (nout == 3) {
         for (int ix = threadIdx.x; ix < nxx; ix += blockDim.x) X[threadIdx.y * ld + ix] = line[ix];
         __syncthreads();
     }
-    // outputs written out in sequence (a loop here costs register spills)
-    auto output = [&](int j, float2* out) {
-        const float2* src = (nout == 3) ? X + threadIdx.y * ld : line;
-        for (int ix = threadIdx.x; ix < nxx; ix += blockDim.x)
-            line[ix] = cscale(src[ix], spec_symbol(a, j, a.kx2[ix] + kzsq) * a.norm);
+    // Outputs written out in sequence (a loop here costs register spills); the
+    // indices are formed again inside each, so that none is held across the
+    // transforms (this keeps the kernel within its register cap).
+    auto output = [&](int j) __attribute__((always_inline)) {
+        const int L = a.L, ld = a.pl.m, nzh = a.nzh, nxx = a.nxx;
+        float2* out = (j == 0) ? a.out0 : (j == 1) ? a.out1 : a.out2;
+        {
+            const int kz = blockIdx.x * L + threadIdx.y;
+            const float kzsq = a.kz2[(kz < nzh) ? kz : 0];
+            float2* ln = smem + threadIdx.y * ld;
+            const float2* src = (a.mode == 0) ? smem + (size_t)(L + threadIdx.y) * ld : ln;
+            for (int ix = threadIdx.x; ix < nxx; ix += blockDim.x)
+                ln[ix] = cscale(src[ix], spec_symbol(a, j, a.kx2[ix] + kzsq) * a.norm);
+        }
         __syncthreads();
         dft_n<+1>(smem, ld, fc, L);
-        for (int g = t0; g < tot; g += nthr) {
-            const int c = g & (L - 1), ix = g >> lg;
-            if (kz0 + c < nzh) out[(size_t)ix * nzh + kz0 + c] = smem[c * ld + ix];
+        const int lgl = 31 - __clz(L), kzb = blockIdx.x * L, tl = L * nxx;
+        for (int g = threadIdx.y * blockDim.x + threadIdx.x; g < tl; g += blockDim.x * blockDim.y) {
+            const int c = g & (L - 1), ix = g >> lgl;
+            if (kzb + c < nzh) out[(size_t)ix * nzh + kzb + c] = smem[c * ld + ix];
         }
         __syncthreads();
     };
-    output(0, a.out0);
+    output(0);
     if (nout == 3) {
-        output(1, a.out1);
-        output(2, a.out2);
+        output(1);
+        output(2);
     }
 }
 
