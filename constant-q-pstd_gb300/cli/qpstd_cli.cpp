@@ -198,7 +198,7 @@ int run_program(Program p, const Options &o) {
 
     qpshim::Common c{tmax, dt, rik.data(), rank, gxp.data(), gzp.data(), nrmx, nx, nz, nxx, nzz, o.pml, par.dx,
                      par.dz, sroffmx, par.disx, nxt, nzt, tracenum.data(), nullptr, fname4.data(), fname5.data(),
-                     par.fd};
+                     par.fd, o.method};
     MultiGPU singpu{shotid.data(), sxp.data(), szp.data()};
     float *models[8] = {vpt.data(), rhot.data(), bbxt.data(), bbzt.data(), nullptr, nullptr, nullptr, nullptr};
     if (visco) models[4] = gamt.data(), models[5] = lamt.data(), models[6] = vwdt.data(), models[7] = taot.data();
@@ -247,7 +247,6 @@ int run_program(Program p, const Options &o) {
                 j.out0.assign((size_t)tmax * std::max(j.s->nr, 1), 0.f);
             }
             if (ok) {
-                j.d.method = o.method;
                 j.id = qpstd_server_submit(sv, &j.d, rtm ? j.obs.data() : nullptr, j.out0.data(),
                                            rtm ? j.out1.data() : nullptr);
                 if (j.id < 0) qpshim::report((int)j.id, j.s->shotid);

@@ -68,6 +68,7 @@ struct Common {
     float *i_bx;
     char *fname4, *fname5;
     float fd = 0.f;  // CPML frequency when known (the native programs); 0: recovered from i_bx
+    int method = QPSTD_FUSED;
 };
 
 // One shot on its window (sgpstd-qmodeling/acps4.cu:312-430).
@@ -135,7 +136,7 @@ inline qpstd_shot_desc describe(const Common &c, Shot &s, int kind, float fd) {
     qpstd_shot_desc d;
     memset(&d, 0, sizeof(d));
     d.kind = kind;
-    d.method = QPSTD_FUSED;
+    d.method = c.method;
     d.nxx = c.nxx;
     d.nzz = c.nzz;
     d.pml = c.pml;

@@ -160,6 +160,16 @@ def test_modeling_program_writes_the_c_abi_gathers(tree, prog, kind, pre):
             assert rel_l2(got, O.OracleShot(d).model().ravel()) < 1e-4
 
 
+@pytest.mark.parametrize("extra", [["--plain"], ["--plain", "--serial"]])
+def test_plain_form_through_the_programs(tree, extra):
+    """The cuFFT plain form (--plain) on both program paths matches the fused gathers."""
+    run(tree, "aps")
+    fused = {s: gather(tree, "reca", s, 41).copy() for s in range(GEOM[0])}
+    run(tree, "aps", *extra)
+    for sid in range(GEOM[0]):
+        assert rel_l2(gather(tree, "reca", sid, 41), fused[sid]) < 1e-5, sid
+
+
 def test_snapshot_output_every_tenth_step(tree):
     d = tree["dir"]
     path = os.path.join(d, "input", "ac2drealmodeling.txt")
