@@ -23,7 +23,8 @@ namespace qp {
 
 // ---- z pass ----------------------------------------------------------------
 // staged fields (each L*2*nzz floats): 0 vz, 1 psi_pz, 2 bbz, 3 psi_vz, 4 Dx
-__global__ void __maxnreg__(QP_PASS_REGS) ac_zpass_kernel(AcZArgs a) {
+template <int RMAX>
+__global__ void __maxnreg__(RMAX == 12 ? QP_Z12_REGS : QP_PASS_REGS) ac_zpass_kernel(AcZArgs a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
     const FFTCtx fc = make_ctx(a.pl, s_pass);
@@ -65,7 +66,7 @@ __global__ void __maxnreg__(QP_PASS_REGS) ac_zpass_kernel(AcZArgs a) {
     if (a.do_v) {
         zload_pair(a.p, line, nzz, has0, has1, r0, r1);
         __syncthreads();
-        roundtrip_conv(smem, ld, fc, L, a.HzP);
+        roundtrip_conv<RMAX>(smem, ld, fc, L, a.HzP);
         if (a.stage) cp_async_wait_all();
         for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
             const float2 d = line[k];
@@ -90,7 +91,7 @@ __global__ void __maxnreg__(QP_PASS_REGS) ac_zpass_kernel(AcZArgs a) {
     }
     if (!a.do_div) return;
     __syncthreads();
-    roundtrip_conv(smem, ld, fc, L, a.HzM);
+    roundtrip_conv<RMAX>(smem, ld, fc, L, a.HzM);
     if (a.stage) cp_async_wait_all();
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 d = line[k];
@@ -111,7 +112,7 @@ __global__ void __maxnreg__(QP_PASS_REGS) ac_zpass_kernel(AcZArgs a) {
         line[k] = dv;
     }
     __syncthreads();
-    roundtrip_conv(smem, ld, fc, L, a.kz2);
+    roundtrip_conv<RMAX>(smem, ld, fc, L, a.kz2);
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 d = line[k];
         if (has0) a.Lz[r0 + k] = d.x;
@@ -307,7 +308,9 @@ size_t ac_xpass_smem(int L, int m, int nxx, int nstaged) {
 
 void launch_ac_zpass(const AcZArgs& a, cudaStream_t s) {
     const int grid = (a.nxx + 2 * a.L - 1) / (2 * a.L);
-    ac_zpass_kernel<<<grid, dim3(a.pl.tx, a.L), ac_zpass_smem(a.L, a.pl.m, a.nzz, a.stage), s>>>(a);
+    const size_t sm = ac_zpass_smem(a.L, a.pl.m, a.nzz, a.stage);
+    if (plan_max_radix(a.pl) <= 12) ac_zpass_kernel<12><<<grid, dim3(a.pl.tx, a.L), sm, s>>>(a);
+    else ac_zpass_kernel<16><<<grid, dim3(a.pl.tx, a.L), sm, s>>>(a);
 }
 
 void launch_ac_xpass(const AcXArgs& a, cudaStream_t s) {
@@ -321,7 +324,8 @@ void launch_ac_xpass(const AcXArgs& a, cudaStream_t s) {
 
 int ac_set_smem_limits() {
     const int lim = QP_SMEM_DYN_MAX;
-    cudaError_t e1 = cudaFuncSetAttribute(ac_zpass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaError_t e1 = cudaFuncSetAttribute(ac_zpass_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    if (e1 == cudaSuccess) e1 = cudaFuncSetAttribute(ac_zpass_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     cudaError_t e2 = cudaFuncSetAttribute(ac_xpass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     cudaError_t e3 = cudaFuncSetAttribute(ac_xpass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     return (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess) ? 0 : -1;

@@ -155,74 +155,94 @@ template <int R, int S> __device__ __forceinline__ void dft(float2 (&v)[R]) {
 
 // ---- one Stockham pass over the lines of the CTA (in place) ------------------------
 // Thread (threadIdx.x, threadIdx.y) handles butterfly j = threadIdx.x of line
-// threadIdx.y.  The radix is a runtime value; all radices share one 16-entry
+// threadIdx.y.  The radix is a runtime value; all radices share one RMAX-entry
 // register array (constant indices under full unrolling), so one copy of the
-// pass serves every plan without register spills.  Ends with a barrier.
-template <int R> __device__ __forceinline__ float2 (&head(float2 (&v)[16]))[R] {
+// pass serves every plan without register spills.  RMAX is 16, or 12 for
+// kernels whose plans use radices up to 12 only (the array then takes 8
+// registers fewer, which lets those kernels run under a lower register cap).
+// Ends with a barrier.
+template <int R, int N> __device__ __forceinline__ float2 (&head(float2 (&v)[N]))[R] {
     return *reinterpret_cast<float2(*)[R]>(&v[0]);
 }
 
-template <int S>
+template <int S, int RMAX = 16>
 __device__ __forceinline__ void reg_pass(float2* buf, int ld, const FFTPass& ps, const float2* __restrict__ tw,
                                          int L) {
+    static_assert(RMAX == 12 || RMAX == 16, "register array of 12 or 16 entries");
     const int R = ps.R;
     const int j = threadIdx.x;
     const int l = threadIdx.y;
     const bool act = (j < ps.B) && (l < L);
-    float2 v[16];
+    float2 v[RMAX];
     int k = 0;
     float2* line = buf + l * ld;
     if (act) {
         k = (ps.ns == 1) ? 0 : (int)(j - __umulhi((unsigned)j, ps.ns_magic) * ps.ns);
 #pragma unroll
-        for (int r = 0; r < 16; r++)
+        for (int r = 0; r < RMAX; r++)
             if (r < R) v[r] = line[j + r * ps.B];
         if (ps.ns > 1) {
             float2 w1 = __ldg(&tw[k * ps.twstride]);
             if (S > 0) w1.y = -w1.y;
             float2 w = w1;
 #pragma unroll
-            for (int r = 1; r < 16; r++)
+            for (int r = 1; r < RMAX; r++)
                 if (r < R) {
                     v[r] = cmul(v[r], w);
                     w = cmul(w, w1);
                 }
         }
-        switch (R) {
-            case 2: dft<2, S>(head<2>(v)); break;
-            case 3: dft<3, S>(head<3>(v)); break;
-            case 4: dft<4, S>(head<4>(v)); break;
-            case 5: dft<5, S>(head<5>(v)); break;
-            case 6: dft<6, S>(head<6>(v)); break;
-            case 7: dft<7, S>(head<7>(v)); break;
-            case 8: dft<8, S>(head<8>(v)); break;
-            case 9: dft<9, S>(head<9>(v)); break;
-            case 10: dft<10, S>(head<10>(v)); break;
-            case 11: dft<11, S>(head<11>(v)); break;
-            case 12: dft<12, S>(head<12>(v)); break;
-            case 13: dft<13, S>(head<13>(v)); break;
-            case 14: dft<14, S>(head<14>(v)); break;
-            case 15: dft<15, S>(head<15>(v)); break;
-            default: dft<16, S>(head<16>(v)); break;
+        if constexpr (RMAX == 16) {
+            switch (R) {
+                case 2: dft<2, S>(head<2>(v)); break;
+                case 3: dft<3, S>(head<3>(v)); break;
+                case 4: dft<4, S>(head<4>(v)); break;
+                case 5: dft<5, S>(head<5>(v)); break;
+                case 6: dft<6, S>(head<6>(v)); break;
+                case 7: dft<7, S>(head<7>(v)); break;
+                case 8: dft<8, S>(head<8>(v)); break;
+                case 9: dft<9, S>(head<9>(v)); break;
+                case 10: dft<10, S>(head<10>(v)); break;
+                case 11: dft<11, S>(head<11>(v)); break;
+                case 12: dft<12, S>(head<12>(v)); break;
+                case 13: dft<13, S>(head<13>(v)); break;
+                case 14: dft<14, S>(head<14>(v)); break;
+                case 15: dft<15, S>(head<15>(v)); break;
+                default: dft<16, S>(head<16>(v)); break;
+            }
+        } else {
+            switch (R) {
+                case 2: dft<2, S>(head<2>(v)); break;
+                case 3: dft<3, S>(head<3>(v)); break;
+                case 4: dft<4, S>(head<4>(v)); break;
+                case 5: dft<5, S>(head<5>(v)); break;
+                case 6: dft<6, S>(head<6>(v)); break;
+                case 7: dft<7, S>(head<7>(v)); break;
+                case 8: dft<8, S>(head<8>(v)); break;
+                case 9: dft<9, S>(head<9>(v)); break;
+                case 10: dft<10, S>(head<10>(v)); break;
+                case 11: dft<11, S>(head<11>(v)); break;
+                default: dft<12, S>(head<12>(v)); break;
+            }
         }
     }
     __syncthreads();
     if (act) {
         const int base = (j - k) * R + k;
 #pragma unroll
-        for (int r = 0; r < 16; r++)
+        for (int r = 0; r < RMAX; r++)
             if (r < R) line[base + r * ps.ns] = v[r];
     }
     __syncthreads();
 }
 
 // Length-m transform (unnormalised) of the L lines, in place.
-template <int S>
+template <int S, int RMAX = 16>
 __device__ __forceinline__ void fft_m_impl(float2* buf, int ld, const FFTPass* __restrict__ sp, int nst,
                                            const float2* __restrict__ tw, int L) {
     for (int i = 0; i < nst; i++) {
         const FFTPass ps = sp[i];
-        reg_pass<S>(buf, ld, ps, tw, L);
+        reg_pass<S, RMAX>(buf, ld, ps, tw, L);
     }
 }
 
@@ -253,15 +273,15 @@ __device__ __forceinline__ FFTCtx make_ctx(const FFTPlanDev& pl, FFTPass* s_pass
     return c;
 }
 
-template <int S> __device__ __forceinline__ void fft_m(float2* buf, int ld, const FFTCtx& pl, int L) {
-    fft_m_impl<S>(buf, ld, pl.sp, pl.nst, pl.w, L);
+template <int S, int RMAX = 16> __device__ __forceinline__ void fft_m(float2* buf, int ld, const FFTCtx& pl, int L) {
+    fft_m_impl<S, RMAX>(buf, ld, pl.sp, pl.nst, pl.w, L);
 }
 
 // Exact length-n DFT of entries [0,n) of each line, in place.  Caller has
 // synchronised after filling buf; ends with a barrier.
-template <int S> __device__ __forceinline__ void dft_n(float2* buf, int ld, const FFTCtx& pl, int L) {
+template <int S, int RMAX = 16> __device__ __forceinline__ void dft_n(float2* buf, int ld, const FFTCtx& pl, int L) {
     if (!pl.blue) {
-        fft_m<S>(buf, ld, pl, L);
+        fft_m<S, RMAX>(buf, ld, pl, L);
         return;
     }
     const int n = pl.n, m = pl.m;
@@ -280,11 +300,11 @@ template <int S> __device__ __forceinline__ void dft_n(float2* buf, int ld, cons
             line[k] = v;
         }
     __syncthreads();
-    fft_m<-1>(buf, ld, pl, L);
+    fft_m<-1, RMAX>(buf, ld, pl, L);
     if (act)
         for (int k = threadIdx.x; k < m; k += blockDim.x) line[k] = cmul(line[k], __ldg(&pl.bhat[k]));
     __syncthreads();
-    fft_m<+1>(buf, ld, pl, L);
+    fft_m<+1, RMAX>(buf, ld, pl, L);
     if (act)
         for (int k = threadIdx.x; k < n; k += blockDim.x) {
             float2 y = cmul(line[k], __ldg(&pl.chirp[k]));
@@ -298,6 +318,7 @@ template <int S> __device__ __forceinline__ void dft_n(float2* buf, int ld, cons
 // plan: y[0,n) = IFFT_m(Hm .* FFT_m(x zero-padded to m)), Hm from conv_table
 // (m = n when n itself is smooth).  Caller has synchronised after filling
 // entries [0,n); ends with a barrier.
+template <int RMAX = 16>
 __device__ __forceinline__ void roundtrip_conv(float2* buf, int ld, const FFTCtx& pl, int L,
                                                const float2* __restrict__ Hm) {
     const int l = threadIdx.y;
@@ -308,11 +329,19 @@ __device__ __forceinline__ void roundtrip_conv(float2* buf, int ld, const FFTCtx
             for (int k = pl.n + threadIdx.x; k < pl.m; k += blockDim.x) line[k] = make_float2(0.f, 0.f);
         __syncthreads();
     }
-    fft_m<-1>(buf, ld, pl, L);
+    fft_m<-1, RMAX>(buf, ld, pl, L);
     if (act)
         for (int k = threadIdx.x; k < pl.m; k += blockDim.x) line[k] = cmul(line[k], __ldg(&Hm[k]));
     __syncthreads();
-    fft_m<+1>(buf, ld, pl, L);
+    fft_m<+1, RMAX>(buf, ld, pl, L);
+}
+
+// Largest radix of a plan (host or device): kernels with plans up to radix 12
+// can run the 12-entry register array.
+__host__ __device__ inline int plan_max_radix(const FFTPlanDev& p) {
+    int r = 0;
+    for (int i = 0; i < p.nst; i++) r = (p.pass[i].R > r) ? p.pass[i].R : r;
+    return r;
 }
 
 // y = IDFT(H .* DFT(x)) with a complex symbol (length n, 1/n folded in).

@@ -34,7 +34,8 @@ namespace qp {
     (void)r1;
 
 // ---- z pass A ---------------------------------------------------------------
-__global__ void __maxnreg__(QP_PASS_REGS) vz_passA_kernel(VzArgsA a) {
+template <int RMAX>
+__global__ void __maxnreg__(RMAX == 12 ? QP_Z12_REGS : QP_PASS_REGS) vz_passA_kernel(VzArgsA a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
     __shared__ FFTPass s_pass_c[QP_MAXST];
@@ -49,7 +50,7 @@ __global__ void __maxnreg__(QP_PASS_REGS) vz_passA_kernel(VzArgsA a) {
     if (a.aux_spec) {
         zrepack(a.aux_spec, line, nzz, nzh, has0, has1, xa);
         __syncthreads();
-        dft_n<+1>(smem, ld, fc, L);
+        dft_n<+1, RMAX>(smem, ld, fc, L);
         for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
             const float2 v = line[k];
             if (has0) a.aux[r0 + k] = v.x;
@@ -59,7 +60,7 @@ __global__ void __maxnreg__(QP_PASS_REGS) vz_passA_kernel(VzArgsA a) {
     }
     zload_pair(a.vz, line, nzz, has0, has1, r0, r1);
     __syncthreads();
-    roundtrip_conv(smem, ld, fcc, L, a.HzM);
+    roundtrip_conv<RMAX>(smem, ld, fcc, L, a.HzM);
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 d = line[k];
         const float ib = a.i_bz[k], ia = a.i_az[k];
@@ -79,7 +80,7 @@ __global__ void __maxnreg__(QP_PASS_REGS) vz_passA_kernel(VzArgsA a) {
         line[k] = dv;
     }
     __syncthreads();
-    dft_n<-1>(smem, ld, fc, L);
+    dft_n<-1, RMAX>(smem, ld, fc, L);
     zunpack(line, a.G, nzz, nzh, has0, has1, xa);
 }
 
@@ -245,7 +246,8 @@ __global__ void __launch_bounds__(768, 1) vz_convtab_kernel(VtabArgs a) {
 }
 
 // ---- z pass B -----------------------------------------------------------------
-__global__ void __maxnreg__(QP_PASS_REGS) vz_passB_kernel(VzArgsB a) {
+template <int RMAX>
+__global__ void __maxnreg__(RMAX == 12 ? QP_Z12_REGS : QP_PASS_REGS) vz_passB_kernel(VzArgsB a) {
     ZPASS_SETUP
     const int nzh = a.nzh;
     float2* acc = smem + (size_t)(L + threadIdx.y) * ld;  // running total of this line pair
@@ -253,7 +255,7 @@ __global__ void __maxnreg__(QP_PASS_REGS) vz_passB_kernel(VzArgsB a) {
     auto term = [&](const float2* spec, const float* cf, float sg, bool first) {
         zrepack(spec, line, nzz, nzh, has0, has1, xa);
         __syncthreads();
-        dft_n<+1>(smem, ld, fc, L);
+        dft_n<+1, RMAX>(smem, ld, fc, L);
         for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
             const float2 y = line[k];
             float2 t = first ? make_float2(0.f, 0.f) : acc[k];
@@ -280,17 +282,18 @@ __global__ void __maxnreg__(QP_PASS_REGS) vz_passB_kernel(VzArgsB a) {
         line[k] = v;
     }
     __syncthreads();
-    dft_n<-1>(smem, ld, fc, L);
+    dft_n<-1, RMAX>(smem, ld, fc, L);
     zunpack(line, a.T, nzz, nzh, has0, has1, xa);
 }
 
 // ---- z pass C -----------------------------------------------------------------
-__global__ void __maxnreg__(QP_PASS_REGS) vz_passC_kernel(VzArgsC a) {
+template <int RMAX>
+__global__ void __maxnreg__(RMAX == 12 ? QP_Z12_REGS : QP_PASS_REGS) vz_passC_kernel(VzArgsC a) {
     ZPASS_SETUP
     const int nzh = a.nzh;
     zrepack(a.Dspec, line, nzz, nzh, has0, has1, xa);
     __syncthreads();
-    dft_n<+1>(smem, ld, fc, L);
+    dft_n<+1, RMAX>(smem, ld, fc, L);
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 D = line[k];
         float2 pn = make_float2(0.f, 0.f);
@@ -340,12 +343,12 @@ __global__ void __maxnreg__(QP_PASS_REGS) vz_passC_kernel(VzArgsC a) {
     __syncthreads();
     // forward z transform of the new p: half spectrum for the aux operator and
     // the staggered z derivative from the same transform
-    dft_n<-1>(smem, ld, fc, L);
+    dft_n<-1, RMAX>(smem, ld, fc, L);
     zunpack(line, a.P, nzz, nzh, has0, has1, xa);
     __syncthreads();
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) line[k] = cmul(line[k], __ldg(&a.HzP[k]));
     __syncthreads();
-    dft_n<+1>(smem, ld, fc, L);
+    dft_n<+1, RMAX>(smem, ld, fc, L);
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 d = line[k];
         const float hb = a.h_bz[k], ha = a.h_az[k];
@@ -365,11 +368,12 @@ __global__ void __maxnreg__(QP_PASS_REGS) vz_passC_kernel(VzArgsC a) {
 }
 
 // ---- z inverse only -------------------------------------------------------------
-__global__ void __maxnreg__(QP_PASS_REGS) vz_zinv_kernel(VzArgsI a) {
+template <int RMAX>
+__global__ void __maxnreg__(RMAX == 12 ? QP_Z12_REGS : QP_PASS_REGS) vz_zinv_kernel(VzArgsI a) {
     ZPASS_SETUP
     zrepack(a.spec, line, nzz, a.nzh, has0, has1, xa);
     __syncthreads();
-    dft_n<+1>(smem, ld, fc, L);
+    dft_n<+1, RMAX>(smem, ld, fc, L);
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 v = line[k];
         if (has0) a.out[r0 + k] = v.x;
@@ -382,7 +386,10 @@ static size_t lsm(int L, int m, int nbuf) { return sizeof(float2) * (size_t)nbuf
 static int zgrid(int nxx, int L) { return (nxx + 2 * L - 1) / (2 * L); }
 
 void launch_vz_passA(const VzArgsA& a, cudaStream_t s) {
-    vz_passA_kernel<<<zgrid(a.nxx, a.L), dim3(max(a.pl.tx, a.plc.tx), a.L), lsm(a.L, max(a.pl.m, a.plc.m), 1), s>>>(a);
+    const dim3 blk(max(a.pl.tx, a.plc.tx), a.L);
+    const size_t sm = lsm(a.L, max(a.pl.m, a.plc.m), 1);
+    if (plan_max_radix(a.pl) <= 12 && plan_max_radix(a.plc) <= 12) vz_passA_kernel<12><<<zgrid(a.nxx, a.L), blk, sm, s>>>(a);
+    else vz_passA_kernel<16><<<zgrid(a.nxx, a.L), blk, sm, s>>>(a);
 }
 void launch_vz_xspec(const VxsArgs& a, cudaStream_t s) {
     vz_xspec_kernel<<<(a.nzh + a.L - 1) / a.L, dim3(a.pl.tx, a.L), lsm(a.L, a.pl.m, a.mode == 0 ? 2 : 1), s>>>(a);
@@ -396,25 +403,35 @@ void launch_vz_convtab(const VtabArgs& a, cudaStream_t s) {
     vz_convtab_kernel<<<(a.nzh + a.L - 1) / a.L, dim3(max(a.pl.tx, a.plc.tx), a.L), lsm(a.L, max(a.pl.m, a.plc.m), 1), s>>>(a);
 }
 void launch_vz_passB(const VzArgsB& a, cudaStream_t s) {
-    vz_passB_kernel<<<zgrid(a.nxx, a.L), dim3(a.pl.tx, a.L), lsm(a.L, a.pl.m, 2), s>>>(a);
+    const dim3 blk(a.pl.tx, a.L);
+    if (plan_max_radix(a.pl) <= 12) vz_passB_kernel<12><<<zgrid(a.nxx, a.L), blk, lsm(a.L, a.pl.m, 2), s>>>(a);
+    else vz_passB_kernel<16><<<zgrid(a.nxx, a.L), blk, lsm(a.L, a.pl.m, 2), s>>>(a);
 }
 void launch_vz_passC(const VzArgsC& a, cudaStream_t s) {
-    vz_passC_kernel<<<zgrid(a.nxx, a.L), dim3(a.pl.tx, a.L), lsm(a.L, a.pl.m, 1), s>>>(a);
+    const dim3 blk(a.pl.tx, a.L);
+    if (plan_max_radix(a.pl) <= 12) vz_passC_kernel<12><<<zgrid(a.nxx, a.L), blk, lsm(a.L, a.pl.m, 1), s>>>(a);
+    else vz_passC_kernel<16><<<zgrid(a.nxx, a.L), blk, lsm(a.L, a.pl.m, 1), s>>>(a);
 }
 void launch_vz_zinv(const VzArgsI& a, cudaStream_t s) {
-    vz_zinv_kernel<<<zgrid(a.nxx, a.L), dim3(a.pl.tx, a.L), lsm(a.L, a.pl.m, 1), s>>>(a);
+    const dim3 blk(a.pl.tx, a.L);
+    if (plan_max_radix(a.pl) <= 12) vz_zinv_kernel<12><<<zgrid(a.nxx, a.L), blk, lsm(a.L, a.pl.m, 1), s>>>(a);
+    else vz_zinv_kernel<16><<<zgrid(a.nxx, a.L), blk, lsm(a.L, a.pl.m, 1), s>>>(a);
 }
 
 int vz_set_smem_limits() {
     int bad = 0;
-    bad |= cudaFuncSetAttribute(vz_passA_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_passA_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_passA_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_xspec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_convtab_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_passB_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_passC_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_zinv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_passB_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_passB_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_passC_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_passC_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_zinv_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_zinv_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     return bad ? -1 : 0;
 }
 
