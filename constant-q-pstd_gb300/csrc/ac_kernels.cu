@@ -24,7 +24,7 @@ namespace qp {
 // ---- z pass ----------------------------------------------------------------
 // staged fields (each L*2*nzz floats): 0 vz, 1 psi_pz, 2 bbz, 3 psi_vz, 4 Dx
 template <int RMAX>
-__global__ void __maxnreg__(RMAX == 12 ? QP_Z12_REGS : QP_PASS_REGS) ac_zpass_kernel(AcZArgs a) {
+__global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) ac_zpass_kernel(AcZArgs a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
     const FFTCtx fc = make_ctx(a.pl, s_pass);
@@ -125,8 +125,9 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_Z12_REGS : QP_PASS_REGS) ac_zpass_ke
 // only the fields of the pass's mode).  Without the p update, the input of the
 // first transform (p, or vx) is its own cp.async group, so the transform starts
 // while the epilogue inputs are still arriving.
-template <bool P>  // P: this launch does the p update (a.do_p)
-__global__ void __maxnreg__(QP_PASS_REGS) ac_xpass_kernel(AcXArgs a) {
+// P: this launch does the p update (a.do_p); RMAX: largest radix of the plan (12 or 16)
+template <bool P, int RMAX>
+__global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) ac_xpass_kernel(AcXArgs a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
     const FFTCtx fc = make_ctx(a.pl, s_pass);
@@ -183,7 +184,7 @@ __global__ void __maxnreg__(QP_PASS_REGS) ac_xpass_kernel(AcXArgs a) {
             if (a.stage) S(0, g) = v;
         }
         __syncthreads();
-        roundtrip_conv(smem, ld, fc, L, a.kx2);
+        roundtrip_conv<RMAX>(smem, ld, fc, L, a.kx2);
         if (a.stage) cp_async_wait_all();
         for (int g = T.t0; g < T.tot; g += T.nthr) {
             int c, ix;
@@ -243,7 +244,7 @@ __global__ void __maxnreg__(QP_PASS_REGS) ac_xpass_kernel(AcXArgs a) {
             }
         }
         __syncthreads();
-        roundtrip_conv(smem, ld, fc, L, a.HxP);
+        roundtrip_conv<RMAX>(smem, ld, fc, L, a.HxP);
         if (a.stage) cp_async_wait_all();
         for (int g = T.t0; g < T.tot; g += T.nthr) {
             int c, ix;
@@ -282,7 +283,7 @@ __global__ void __maxnreg__(QP_PASS_REGS) ac_xpass_kernel(AcXArgs a) {
             }
         }
         __syncthreads();
-        roundtrip_conv(smem, ld, fc, L, a.HxM);
+        roundtrip_conv<RMAX>(smem, ld, fc, L, a.HxM);
         if (a.stage) cp_async_wait_all();
         for (int g = T.t0; g < T.tot; g += T.nthr) {
             int c, ix;
@@ -318,16 +319,22 @@ void launch_ac_xpass(const AcXArgs& a, cudaStream_t s) {
     const int nst = a.stage ? xstage_count(xstage_fields(a.do_p, a.do_v, a.do_dx)) : 0;
     const size_t sm = ac_xpass_smem(a.L, a.pl.m, a.nxx, nst);
     // the instance without the p update carries only the transforms it runs
-    if (a.do_p) ac_xpass_kernel<true><<<grid, dim3(a.pl.tx, a.L), sm, s>>>(a);
-    else ac_xpass_kernel<false><<<grid, dim3(a.pl.tx, a.L), sm, s>>>(a);
+    const dim3 blk(a.pl.tx, a.L);
+    const bool r12 = plan_max_radix(a.pl) <= 12;
+    if (a.do_p && r12) ac_xpass_kernel<true, 12><<<grid, blk, sm, s>>>(a);
+    else if (a.do_p) ac_xpass_kernel<true, 16><<<grid, blk, sm, s>>>(a);
+    else if (r12) ac_xpass_kernel<false, 12><<<grid, blk, sm, s>>>(a);
+    else ac_xpass_kernel<false, 16><<<grid, blk, sm, s>>>(a);
 }
 
 int ac_set_smem_limits() {
     const int lim = QP_SMEM_DYN_MAX;
     cudaError_t e1 = cudaFuncSetAttribute(ac_zpass_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     if (e1 == cudaSuccess) e1 = cudaFuncSetAttribute(ac_zpass_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-    cudaError_t e2 = cudaFuncSetAttribute(ac_xpass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-    cudaError_t e3 = cudaFuncSetAttribute(ac_xpass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaError_t e2 = cudaFuncSetAttribute(ac_xpass_kernel<true, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    if (e2 == cudaSuccess) e2 = cudaFuncSetAttribute(ac_xpass_kernel<true, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaError_t e3 = cudaFuncSetAttribute(ac_xpass_kernel<false, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    if (e3 == cudaSuccess) e3 = cudaFuncSetAttribute(ac_xpass_kernel<false, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     return (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess) ? 0 : -1;
 }
 

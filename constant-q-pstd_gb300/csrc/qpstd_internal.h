@@ -14,9 +14,9 @@
 // x-spectral pass (Bluestein transforms and the Q-RTM filter's exponentials)
 // spills below 72 and takes that cap.
 #define QP_PASS_REGS 56
-// z passes whose plans use radices up to 12 run a 12-entry register array
+// Passes whose plans use radices up to 12 run a 12-entry register array
 // (fft_reg.cuh) and fit 44 registers spill-free: 11 (not 9) 128-thread CTAs per SM.
-#define QP_Z12_REGS 44
+#define QP_R12_REGS 44
 #define QP_WIDE_REGS 80
 #define QP_EXACT_REGS 72
 // Dynamic shared memory a pass kernel may request: the 227 KB per-CTA opt-in

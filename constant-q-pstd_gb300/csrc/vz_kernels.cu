@@ -35,7 +35,7 @@ namespace qp {
 
 // ---- z pass A ---------------------------------------------------------------
 template <int RMAX>
-__global__ void __maxnreg__(RMAX == 12 ? QP_Z12_REGS : QP_PASS_REGS) vz_passA_kernel(VzArgsA a) {
+__global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passA_kernel(VzArgsA a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
     __shared__ FFTPass s_pass_c[QP_MAXST];
@@ -158,8 +158,9 @@ __global__ void __maxnreg__(QP_EXACT_REGS) vz_xspec_kernel(VxsArgs a) {
 // replaces the exact (Bluestein) DFTs: one forward transform, then per output a
 // multiply by the column's table and one inverse transform.
 // NOUT = 3 (mode 0) or 1 (mode 1): each instance carries only the transforms it runs.
-template <int NOUT>
-__global__ void __maxnreg__(NOUT == 1 ? QP_PASS_REGS : QP_WIDE_REGS)
+// RMAX: largest radix of the convolution plan (12 or 16).
+template <int NOUT, int RMAX>
+__global__ void __maxnreg__(NOUT == 3 ? QP_WIDE_REGS : RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS)
     vz_xspec_conv_kernel(VxsArgs a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
@@ -179,7 +180,7 @@ __global__ void __maxnreg__(NOUT == 1 ? QP_PASS_REGS : QP_WIDE_REGS)
     }
     for (int k = nxx + threadIdx.x; k < m; k += blockDim.x) line[k] = make_float2(0.f, 0.f);
     __syncthreads();
-    fft_m<-1>(smem, ld, fc, L);
+    fft_m<-1, RMAX>(smem, ld, fc, L);
     const int kz = min(kz0 + (int)threadIdx.y, nzh - 1);
     if (nout == 3) {
         for (int k = threadIdx.x; k < m; k += blockDim.x) X[threadIdx.y * ld + k] = line[k];
@@ -192,7 +193,7 @@ __global__ void __maxnreg__(NOUT == 1 ? QP_PASS_REGS : QP_WIDE_REGS)
         const float* tk = tab + (size_t)kz * mh;
         for (int k = threadIdx.x; k < m; k += blockDim.x) line[k] = cscale(src[k], __ldg(&tk[min(k, m - k)]));
         __syncthreads();
-        fft_m<+1>(smem, ld, fc, L);
+        fft_m<+1, RMAX>(smem, ld, fc, L);
         for (int g = t0; g < tot; g += nthr) {
             const int c = g & (L - 1), ix = g >> lg;
             if (kz0 + c < nzh) out[(size_t)ix * nzh + kz0 + c] = smem[c * ld + ix];
@@ -247,7 +248,7 @@ __global__ void __launch_bounds__(768, 1) vz_convtab_kernel(VtabArgs a) {
 
 // ---- z pass B -----------------------------------------------------------------
 template <int RMAX>
-__global__ void __maxnreg__(RMAX == 12 ? QP_Z12_REGS : QP_PASS_REGS) vz_passB_kernel(VzArgsB a) {
+__global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passB_kernel(VzArgsB a) {
     ZPASS_SETUP
     const int nzh = a.nzh;
     float2* acc = smem + (size_t)(L + threadIdx.y) * ld;  // running total of this line pair
@@ -288,7 +289,7 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_Z12_REGS : QP_PASS_REGS) vz_passB_ke
 
 // ---- z pass C -----------------------------------------------------------------
 template <int RMAX>
-__global__ void __maxnreg__(RMAX == 12 ? QP_Z12_REGS : QP_PASS_REGS) vz_passC_kernel(VzArgsC a) {
+__global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passC_kernel(VzArgsC a) {
     ZPASS_SETUP
     const int nzh = a.nzh;
     zrepack(a.Dspec, line, nzz, nzh, has0, has1, xa);
@@ -369,7 +370,7 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_Z12_REGS : QP_PASS_REGS) vz_passC_ke
 
 // ---- z inverse only -------------------------------------------------------------
 template <int RMAX>
-__global__ void __maxnreg__(RMAX == 12 ? QP_Z12_REGS : QP_PASS_REGS) vz_zinv_kernel(VzArgsI a) {
+__global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) vz_zinv_kernel(VzArgsI a) {
     ZPASS_SETUP
     zrepack(a.spec, line, nzz, a.nzh, has0, has1, xa);
     __syncthreads();
@@ -396,8 +397,12 @@ void launch_vz_xspec(const VxsArgs& a, cudaStream_t s) {
 }
 void launch_vz_xspec_conv(const VxsArgs& a, cudaStream_t s) {
     const int grid = (a.nzh + a.L - 1) / a.L;
-    if (a.mode == 0) vz_xspec_conv_kernel<3><<<grid, dim3(a.plc.tx, a.L), lsm(a.L, a.plc.m, 2), s>>>(a);
-    else vz_xspec_conv_kernel<1><<<grid, dim3(a.plc.tx, a.L), lsm(a.L, a.plc.m, 1), s>>>(a);
+    const dim3 blk(a.plc.tx, a.L);
+    const bool r12 = plan_max_radix(a.plc) <= 12;
+    if (a.mode == 0 && r12) vz_xspec_conv_kernel<3, 12><<<grid, blk, lsm(a.L, a.plc.m, 2), s>>>(a);
+    else if (a.mode == 0) vz_xspec_conv_kernel<3, 16><<<grid, blk, lsm(a.L, a.plc.m, 2), s>>>(a);
+    else if (r12) vz_xspec_conv_kernel<1, 12><<<grid, blk, lsm(a.L, a.plc.m, 1), s>>>(a);
+    else vz_xspec_conv_kernel<1, 16><<<grid, blk, lsm(a.L, a.plc.m, 1), s>>>(a);
 }
 void launch_vz_convtab(const VtabArgs& a, cudaStream_t s) {
     vz_convtab_kernel<<<(a.nzh + a.L - 1) / a.L, dim3(max(a.pl.tx, a.plc.tx), a.L), lsm(a.L, max(a.pl.m, a.plc.m), 1), s>>>(a);
@@ -423,8 +428,10 @@ int vz_set_smem_limits() {
     bad |= cudaFuncSetAttribute(vz_passA_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_passA_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_xspec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<3, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<3, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<1, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<1, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_convtab_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_passB_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_passB_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
