@@ -99,7 +99,9 @@ __device__ __forceinline__ float spec_symbol(const VxsArgs& a, int j, float k2) 
     return ka - num / den;
 }
 
-__global__ void __maxnreg__(QP_EXACT_REGS) vz_xspec_kernel(VxsArgs a) {
+// RMAX: largest radix of the exact plan (12 or 16; Bluestein plans included).
+template <int RMAX>
+__global__ void __maxnreg__(RMAX == 12 ? QP_PASS_REGS : QP_EXACT_REGS) vz_xspec_kernel(VxsArgs a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
     const FFTCtx fc = make_ctx(a.pl, s_pass);
@@ -117,7 +119,7 @@ __global__ void __maxnreg__(QP_EXACT_REGS) vz_xspec_kernel(VxsArgs a) {
         smem[c * ld + ix] = (kz < nzh) ? a.in[(size_t)ix * nzh + kz] : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    dft_n<-1>(smem, ld, fc, L);
+    dft_n<-1, RMAX>(smem, ld, fc, L);
     if (nout == 3) {
         for (int ix = threadIdx.x; ix < nxx; ix += blockDim.x) X[threadIdx.y * ld + ix] = line[ix];
         __syncthreads();
@@ -137,7 +139,7 @@ __global__ void __maxnreg__(QP_EXACT_REGS) vz_xspec_kernel(VxsArgs a) {
                 ln[ix] = cscale(src[ix], spec_symbol(a, j, a.kx2[ix] + kzsq) * a.norm);
         }
         __syncthreads();
-        dft_n<+1>(smem, ld, fc, L);
+        dft_n<+1, RMAX>(smem, ld, fc, L);
         const int lgl = 31 - __clz(L), kzb = blockIdx.x * L, tl = L * nxx;
         for (int g = threadIdx.y * blockDim.x + threadIdx.x; g < tl; g += blockDim.x * blockDim.y) {
             const int c = g & (L - 1), ix = g >> lgl;
@@ -393,7 +395,10 @@ void launch_vz_passA(const VzArgsA& a, cudaStream_t s) {
     else vz_passA_kernel<16><<<zgrid(a.nxx, a.L), blk, sm, s>>>(a);
 }
 void launch_vz_xspec(const VxsArgs& a, cudaStream_t s) {
-    vz_xspec_kernel<<<(a.nzh + a.L - 1) / a.L, dim3(a.pl.tx, a.L), lsm(a.L, a.pl.m, a.mode == 0 ? 2 : 1), s>>>(a);
+    const int grid = (a.nzh + a.L - 1) / a.L;
+    const size_t sm = lsm(a.L, a.pl.m, a.mode == 0 ? 2 : 1);
+    if (plan_max_radix(a.pl) <= 12) vz_xspec_kernel<12><<<grid, dim3(a.pl.tx, a.L), sm, s>>>(a);
+    else vz_xspec_kernel<16><<<grid, dim3(a.pl.tx, a.L), sm, s>>>(a);
 }
 void launch_vz_xspec_conv(const VxsArgs& a, cudaStream_t s) {
     const int grid = (a.nzh + a.L - 1) / a.L;
@@ -427,7 +432,8 @@ int vz_set_smem_limits() {
     int bad = 0;
     bad |= cudaFuncSetAttribute(vz_passA_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_passA_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_xspec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_xspec_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_xspec_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<3, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<3, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<1, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
