@@ -142,13 +142,20 @@ static bool smooth7(int v) {
 
 // Radices of the register passes (each 2..16): fewest passes first, then the
 // largest smallest radix, since a pass of radix R keeps m/R threads per line
-// busy (5184 -> 9,9,8,8 runs on 648 threads; 1728 -> 12,12,12 on 144).
+// busy (5184 -> 9,9,8,8 runs on 648 threads; 1728 -> 12,12,12 on 144), then
+// the smaller largest radix (a plan with radices up to 12 runs the kernels'
+// 12-entry register array, in fewer registers).
 static void factor_search(int v, int maxr, std::vector<int>& cur, std::vector<int>& best) {
     if (v == 1) {
-        if (best.empty() || cur.size() < best.size() ||
-            (cur.size() == best.size() && *std::min_element(cur.begin(), cur.end()) >
-                                              *std::min_element(best.begin(), best.end())))
+        if (best.empty() || cur.size() < best.size()) {
             best = cur;
+        } else if (cur.size() == best.size()) {
+            const int cmin = *std::min_element(cur.begin(), cur.end());
+            const int bmin = *std::min_element(best.begin(), best.end());
+            const int cmax = *std::max_element(cur.begin(), cur.end());
+            const int bmax = *std::max_element(best.begin(), best.end());
+            if (cmin > bmin || (cmin == bmin && cmax < bmax)) best = cur;
+        }
         return;
     }
     if (!best.empty() && cur.size() + 1 > best.size()) return;
@@ -158,6 +165,13 @@ static void factor_search(int v, int maxr, std::vector<int>& cur, std::vector<in
         factor_search(v / r, r, cur, best);  // non-increasing radices: each multiset once
         cur.pop_back();
     }
+}
+
+// Relative cost of a length whose plan has radices up to 12: the pass kernels
+// then run at 44 instead of 56 registers per thread (qpstd_internal.h), which
+// is worth a slightly longer transform when several lengths are admissible.
+static double radix_weight(const std::vector<int>& rad) {
+    return (*std::max_element(rad.begin(), rad.end()) <= 12) ? 0.85 : 1.0;
 }
 
 static bool factor_direct(int n, std::vector<int>& rad) {
@@ -216,14 +230,14 @@ int build_plan_host(int n, HostPlan& hp) {
         hp.m = n;
     } else {
         // Bluestein: the {2,3,5,7}-smooth inner length in [2n-1, 2.3n] with the
-        // lowest pass work, m * (passes + 1)
+        // lowest pass work, m * (passes + 1), weighted by radix_weight
         hp.blue = 1;
         double best = 1e300;
         for (int m = 2 * n - 1; m <= (int)(2.3 * n) + 8; m++) {
             if (!smooth7(m)) continue;
             std::vector<int> r;
             if (!factor_direct(m, r)) continue;
-            const double cost = (double)m * (r.size() + 1);
+            const double cost = (double)m * (r.size() + 1) * radix_weight(r);
             if (cost < best) {
                 best = cost;
                 hp.m = m;
@@ -274,7 +288,7 @@ int build_conv_plan_host(int n, HostPlan& hp) {
             if (!smooth7(m)) continue;
             std::vector<int> r;
             if (!factor_direct(m, r)) continue;
-            const double cost = (double)m * r.size();
+            const double cost = (double)m * r.size() * radix_weight(r);
             if (cost < best) {
                 best = cost;
                 hp.m = m;
