@@ -397,7 +397,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="qrtm4")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--e2e-shots", type=int, default=8)
+    ap.add_argument("--e2e-shots", type=int, default=16)
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--shots", type=int, default=0,

@@ -3,8 +3,8 @@
 #include <cuda_runtime.h>
 
 #define QP_MAXST 10
-// Threads per CTA of the pass kernels (__launch_bounds__(QP_MAXTHREADS, 1):
-// 80 registers per thread, enough for the radix-16 butterflies).
+// Threads per CTA of the pass kernels.  Kernels without a register cap below
+// declare __launch_bounds__(QP_MAXTHREADS, 1), i.e. up to 80 registers.
 #define QP_MAXTHREADS 768
 // Register cap of the step's pass kernels: at 56 they compile spill-free and hold
 // 4 (not 3) 256-thread line CTAs, or 9 (not 8) 128-thread ones, per SM, which
