@@ -7,7 +7,7 @@
 // declare __launch_bounds__(QP_MAXTHREADS, 1), i.e. up to 80 registers.
 #define QP_MAXTHREADS 768
 // Register cap of the step's pass kernels: at 56 they compile spill-free and hold
-// 4 (not 3) 256-thread line CTAs, or 8 (not 7) 128-thread ones, per SM (registers
+// 4 (not 3) 256-thread line CTAs, or 9 (not 8) 128-thread ones, per SM (registers
 // are allocated per warp in units of 256), which matters when many shots share
 // the GPU.  The three-output x-spectral pass keeps
 // 80: capped, it measured slower (at 56 without spills, four of its 54 KB CTAs per
@@ -16,7 +16,7 @@
 // spills below 72 and takes that cap.
 #define QP_PASS_REGS 56
 // Passes whose plans use radices up to 12 run a 12-entry register array
-// (fft_reg.cuh) and fit 44 registers spill-free: 10 (not 8) 128-thread CTAs per SM.
+// (fft_reg.cuh) and fit 44 registers spill-free: 10 (not 9) 128-thread CTAs per SM.
 #define QP_R12_REGS 44
 #define QP_WIDE_REGS 80
 #define QP_EXACT_REGS 72
