@@ -168,7 +168,7 @@ static void factor_search(int v, int maxr, std::vector<int>& cur, std::vector<in
 }
 
 // Relative cost of a length whose plan has radices up to 12: the pass kernels
-// then run at 44 instead of 56 registers per thread (qpstd_internal.h), which
+// then run at 48 instead of 56 registers per thread (qpstd_internal.h), which
 // is worth a slightly longer transform when several lengths are admissible.
 static double radix_weight(const std::vector<int>& rad) {
     return (*std::max_element(rad.begin(), rad.end()) <= 12) ? 0.85 : 1.0;
