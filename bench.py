@@ -41,6 +41,8 @@ METRIC = "Q-RTM shots/hr batched vs per-shot @relL2≤1e-4; Gpts/s; HBM GB/s; p5
 # Algorithmic bytes per padded grid point per time step (every state field
 # read and written once, every model field read once): acoustic 72 B
 # (7 state x 8 + 4 model x 4), constant-Q 96 B (8 state x 8 + 8 model x 4).
+# spin ahead of a flushed timed step: 2 ms at the 2070 MHz SM clock
+HOLD_CYCLES = 4_140_000
 ALG_BYTES_STEP = {"aps": 72.0, "artm": 72.0, "vaps": 96.0, "qrtm": 96.0}
 
 
@@ -468,8 +470,16 @@ def main():
             # working set near L2: flush it (untimed) before every timed step
             flush.fill_(float(i))
             torch.cuda.synchronize()
+            # a spin kernel ahead of the step keeps the GPU busy while the host
+            # enqueues the step, so the events time the step's kernels and not the
+            # host's launch latency (a shot's steps run with the host ahead of the
+            # GPU); the other shot streams start at the same event
+            with torch.cuda.stream(streams[0]):
+                torch.cuda._sleep(HOLD_CYCLES)
             e0 = torch.cuda.Event(enable_timing=True)
             e0.record(streams[0])
+            for s in streams[1:]:
+                s.wait_event(e0)
             B.pipeline_step(t, last=(i == args.steps - 1))
             ends = []
             for s in streams:
@@ -532,7 +542,8 @@ def main():
         "dtype": "f32",
         "data": f"synthetic (seeded layered model, seed {seed})",
         "config": dict(desc, points_per_step=pts,
-                       l2="flushed (512 MB write) between timed steps, one step per timing"
+                       l2="flushed (512 MB write) between timed steps, one step per timing, "
+                          "enqueued behind a 2 ms spin kernel"
                        if flush is not None
                        else f"working set {pts * 4 * 30 / 1e9:.1f} GB >> 129 MB L2, no flush; "
                             f"the {args.steps} steps timed back to back",
