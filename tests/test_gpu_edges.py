@@ -1,0 +1,73 @@
+"""Edge cases of the fused path against the FP64 oracle (GPU): receivers on the
+padded grid's corners and repeated at one point, shots without receivers, and a
+source inside the CPML corner, on odd grids (the last z and x line pairs hold one
+line).  Tolerance: relative L2 <= 1e-4 against FP64, as for the other parity tests.
+The shots run 300 steps, as the other state comparisons do: the CPML memory
+fields are compared once the wavefield has filled the CPML (at its first arrival
+they are small, and the FP32 rounding of the leading edge weighs more in their
+norm: fipx measured 1.4e-4 after 160 steps on the 57 x 33 model).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+import qpstd
+from cases import rel_l2, small_shot
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    qpstd.lib()
+
+
+def _nfields(kind):
+    """State fields compared: p, vx, vz, fipx, fipz, fivxx, fivzz, plus the
+    auxiliary field that only the viscoacoustic kinds use."""
+    return 8 if kind == qpstd.VAPS else 7
+
+
+def _corner_receivers(d):
+    nxx, nzz = d["nxx"], d["nzz"]
+    gx = [0, nxx - 1, 0, nxx - 1, d["xsg"], d["xsg"], nxx // 2]
+    gz = [0, 0, nzz - 1, nzz - 1, nzz - 1, nzz - 1, d["zsg"]]
+    return dict(d, gxg=np.array(gx, dtype=np.int32), gzg=np.array(gz, dtype=np.int32))
+
+
+@pytest.mark.parametrize("kind", [qpstd.APS, qpstd.VAPS])
+def test_receivers_on_corners_and_repeated(kind):
+    d = _corner_receivers(small_shot(kind, nx=57, nz=33, nt=300))
+    ref_g, ref_st = O.OracleShot(d).model(want_state=True)
+    g, st = qpstd.model_shot(d, want_state=True)
+    assert g.shape == (300, 7)
+    # a repeated receiver records the same trace twice, bit for bit
+    assert np.array_equal(g[:, 4], g[:, 5])
+    # corner traces are small (inside the CPML): compare the whole gather, and
+    # the interior trace on its own
+    assert rel_l2(g, ref_g) < TOL
+    assert rel_l2(g[:, 6], ref_g[:, 6]) < TOL
+    for f in range(_nfields(kind)):
+        assert rel_l2(st[f], ref_st[f]) < TOL, f
+
+
+@pytest.mark.parametrize("kind", [qpstd.APS, qpstd.VAPS])
+def test_shot_without_receivers(kind):
+    d = small_shot(kind, nx=57, nz=33, nt=300)
+    d = dict(d, gxg=np.zeros(0, dtype=np.int32), gzg=np.zeros(0, dtype=np.int32))
+    ref_g, ref_st = O.OracleShot(d).model(want_state=True)
+    g, st = qpstd.model_shot(d, want_state=True)
+    assert g.shape == (300, 0)
+    for f in range(_nfields(kind)):
+        assert rel_l2(st[f], ref_st[f]) < TOL, f
+
+
+def test_source_in_the_cpml_corner():
+    d = small_shot(qpstd.APS, nx=57, nz=33, nt=300)
+    d = dict(d, xsg=2, zsg=d["nzz"] - 3)
+    ref_g, ref_st = O.OracleShot(d).model(want_state=True)
+    g, st = qpstd.model_shot(d, want_state=True)
+    assert rel_l2(g, ref_g) < TOL
+    for f in range(_nfields(qpstd.APS)):
+        assert rel_l2(st[f], ref_st[f]) < TOL, f
