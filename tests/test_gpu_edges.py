@@ -31,8 +31,9 @@ def _nfields(kind):
 
 def _corner_receivers(d):
     nxx, nzz = d["nxx"], d["nzz"]
-    gx = [0, nxx - 1, 0, nxx - 1, d["xsg"], d["xsg"], nxx // 2]
-    gz = [0, 0, nzz - 1, nzz - 1, nzz - 1, nzz - 1, d["zsg"]]
+    # four corners, two receivers at one interior point, one interior receiver
+    gx = [0, nxx - 1, 0, nxx - 1, nxx // 2 + 5, nxx // 2 + 5, nxx // 2]
+    gz = [0, 0, nzz - 1, nzz - 1, d["zsg"], d["zsg"], d["zsg"]]
     return dict(d, gxg=np.array(gx, dtype=np.int32), gzg=np.array(gz, dtype=np.int32))
 
 
@@ -71,3 +72,21 @@ def test_source_in_the_cpml_corner():
     assert rel_l2(g, ref_g) < TOL
     for f in range(_nfields(qpstd.APS)):
         assert rel_l2(st[f], ref_st[f]) < TOL, f
+
+
+@pytest.mark.parametrize("kind,fwd", [(qpstd.ARTM, O.APS), (qpstd.QRTM, O.VAPS)])
+def test_rtm_with_corner_and_repeated_receivers(kind, fwd):
+    """The receiver side injects the observed traces at the receivers: two
+    receivers at one point both add (a collision of the injection), and the
+    corner receivers inject inside the CPML."""
+    d = _corner_receivers(small_shot(kind, nx=57, nz=33, nt=200, snaps=6))
+    obs = O.OracleShot(dict(d, kind=fwd)).model()
+    ref_img, ref_ssg, _ = O.OracleShot(d).rtm(obs)
+    img, ssg = qpstd.rtm_shot(d, obs)
+    assert rel_l2(ssg, ref_ssg) < TOL
+    assert rel_l2(img, ref_img) < TOL
+    # the repeated receiver's trace counts twice: dropping one copy changes the image
+    obs1 = obs.copy()
+    obs1[:, 5] = 0.0
+    ref_img1, _, _ = O.OracleShot(d).rtm(obs1)
+    assert rel_l2(ref_img1, ref_img) > 10 * TOL
