@@ -12,6 +12,7 @@ import pytest
 
 import oracle as O
 import qpstd
+import workloads as W
 from cases import rel_l2, small_shot
 
 pytestmark = pytest.mark.gpu
@@ -95,3 +96,26 @@ def test_rtm_with_corner_and_repeated_receivers(kind, fwd):
     obs5[:, 5] = 0.0
     ref_img5, _, _ = O.OracleShot(d).rtm(obs5)
     assert rel_l2(ref_img5, ref_img) > 10 * TOL
+
+
+@pytest.mark.parametrize("bad,msg", [("source", "shot grid index"), ("receiver", "receiver grid index"),
+                                     ("snaps", "snaps"), ("width", None)])
+def test_bad_shots_return_a_status(bad, msg):
+    """Where the reference prints and exits, the library returns a status (the
+    Python binding raises), launches nothing, and stays usable."""
+    d = small_shot(qpstd.APS, nx=57, nz=33, nt=20)
+    if bad == "source":
+        d = dict(d, xsg=d["nxx"])
+    elif bad == "receiver":
+        d = dict(d, gzg=np.full_like(d["gzg"], -1))
+    elif bad == "snaps":
+        d = dict(small_shot(qpstd.ARTM, nx=57, nz=33, nt=20), snaps=65)
+    else:  # padded width 4117: longer than one CTA's line in the fused form
+        d = W.make_shot(qpstd.APS, 4096, 24, 10, 20, 0.0005, 25.0, seed=9)
+    with pytest.raises(qpstd.QpstdError, match=msg):
+        if bad == "snaps":
+            qpstd.rtm_shot(d, np.zeros((20, d["gxg"].size), dtype=np.float32))
+        else:
+            qpstd.model_shot(d)
+    good = small_shot(qpstd.APS, nx=57, nz=33, nt=40)
+    assert rel_l2(qpstd.model_shot(good), O.OracleShot(good).model()) < TOL
