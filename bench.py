@@ -46,27 +46,6 @@ HOLD_CYCLES = 4_140_000
 ALG_BYTES_STEP = {"aps": 72.0, "artm": 72.0, "vaps": 96.0, "qrtm": 96.0}
 
 
-def synthetic_obs(d: dict, seed: int) -> np.ndarray:
-    """Observed data with the shape of a Q-RTM gather (nt x nr): a few
-    hyperbolic reflections of the source wavelet.  The cost of RTM does not
-    depend on the values, so the batch does not need 64 modeling runs."""
-    import workloads as W
-    rng = np.random.default_rng(seed)
-    nt, nr, dt = d["nt"], len(d["gxg"]), d["dt"]
-    w = W.ricker(nt, dt, d["fd"])
-    off = (np.asarray(d["gxg"]) - d["xsg"]) * d["dx"]
-    obs = np.zeros((nt, nr))
-    t = np.arange(nt) * dt
-    for _ in range(4):
-        t0, v = rng.uniform(0.2, 1.8), rng.uniform(1800.0, 4000.0)
-        tr = np.sqrt(t0 ** 2 + (off / v) ** 2)
-        idx = np.clip(np.rint(tr / dt).astype(int), 0, nt - 1)
-        for j in range(nr):
-            k = idx[j]
-            obs[k:, j] += rng.uniform(-1, 1) * w[: nt - k]
-    return obs.astype(np.float32)
-
-
 def workload(name: str):
     """(shots, kind name, seed, description, obs maker)"""
     import qpstd
@@ -74,23 +53,15 @@ def workload(name: str):
 
     if name == "qrtm4":
         seed = 1004
-        rng = np.random.default_rng(seed)
-        parent = W.parent_model(6000, 600, seed, nlayers=12, nanom=3)
-        shots = []
-        for i in range(64):
-            nx = int(rng.integers(600, 2001))
-            x0 = int(rng.integers(0, 6000 - nx + 1))
-            shots.append(W.window_of_parent(qpstd.QRTM, parent, x0, nx, 30, 5000, 0.0005, 20.0, 30))
+        shots = W.qrtm4_shots(5000, 30, 64, seed, qpstd.QRTM)
         desc = {"workload": "qrtm4", "kind": "qrtm", "shots": 64, "nz": 600,
                 "nx_range": [min(d["nxx"] - 60 for d in shots), max(d["nxx"] - 60 for d in shots)],
                 "pml": 30, "nt": 5000, "dt": 0.0005, "snaps": 30, "form": "power-expansion (executed reference form)",
                 "obs": "synthetic hyperbolic events (RTM cost is data-independent)"}
-        return shots, "qrtm", seed, desc, lambda d, i: synthetic_obs(d, seed + i)
+        return shots, "qrtm", seed, desc, lambda d, i: W.synthetic_obs(d, seed + i)
     if name == "artm3":
         seed = 1003
-        d = W.make_shot(2, 2400, 800, 30, 6000, 0.0005, 20.0, seed=seed, nlayers=12, nanom=3,
-                        smooth_cells=8.0, snaps=40)
-        true = W.make_shot(0, 2400, 800, 30, 6000, 0.0005, 20.0, seed=seed, nlayers=12, nanom=3)
+        d, true = W.artm3_shots(6000, 40, seed)
         desc = {"workload": "artm3", "kind": "artm", "shots": 1, "grid": [d["nxx"], d["nzz"]], "nt": 6000,
                 "snaps": 40, "receivers": int(len(d["gxg"])), "obs": "fused aps modeling on the unsmoothed model"}
         return [d], "artm", seed, desc, lambda dd, i: qpstd.model_shot(true)
@@ -320,7 +291,7 @@ def run_serve(args, ws, rank):
     for (k, nx, nz, nt, s) in reqs:
         d = W.make_shot(k, nx, nz, 20, nt, 0.0005, 20.0, s, nlayers=6, nanom=1, snaps=30)
         shots.append(d)
-        obs.append(synthetic_obs(d, s) if k in (qpstd.ARTM, qpstd.QRTM) else None)
+        obs.append(W.synthetic_obs(d, s) if k in (qpstd.ARTM, qpstd.QRTM) else None)
     pts = np.array([d["nxx"] * d["nzz"] for d in shots], dtype=np.float64)
     cnt = np.array([d["nt"] * (2 if d["kind"] in (qpstd.ARTM, qpstd.QRTM) else 1) for d in shots], dtype=np.float64)
     work = float((pts * cnt).sum())

@@ -336,14 +336,6 @@ __device__ __forceinline__ void roundtrip_conv(float2* buf, int ld, const FFTCtx
     fft_m<+1, RMAX>(buf, ld, pl, L);
 }
 
-// Largest radix of a plan (host or device): kernels with plans up to radix 12
-// can run the 12-entry register array.
-__host__ __device__ inline int plan_max_radix(const FFTPlanDev& p) {
-    int r = 0;
-    for (int i = 0; i < p.nst; i++) r = (p.pass[i].R > r) ? p.pass[i].R : r;
-    return r;
-}
-
 // y = IDFT(H .* DFT(x)) with a complex symbol (length n, 1/n folded in).
 __device__ __forceinline__ void roundtrip_c(float2* buf, int ld, const FFTCtx& pl, int L,
                                             const float2* __restrict__ H) {

@@ -1,9 +1,10 @@
 // noalloc.cu -- acoustic time steps that allocate no device memory.
 //
-// Some callers cannot call cudaMalloc: code that runs while another part of the
-// process is capturing a CUDA graph, plug-ins that may only touch the buffers
-// their host hands them, and hosts whose device memory is owned by a pool they
-// do not control.  For them, qpstd_ac_advance_noalloc runs the fused acoustic
+// Some callers cannot call cudaMalloc: plug-ins that may only touch the buffers
+// their host application hands them, hosts whose device memory all belongs to a
+// pool they do not control, and callers on a latency-critical path where an
+// allocation (and the implicit device synchronisation cudaFree brings) is not
+// allowed.  For them, qpstd_ac_advance_noalloc runs the fused acoustic
 // step (the same z and x pass kernels as qpstd_shot_advance) with all of its
 // scratch -- the carried x divergence, div, the z part of the Laplacian, the
 // per-point coefficients, the FFT and convolution tables, the CPML profiles
@@ -97,15 +98,22 @@ const float* put_real(TableImage& im, const std::vector<double>& v) {
     return p;
 }
 
-// Device view of a convolution plan whose twiddles live in the image.
-bool put_plan(TableImage& im, const HostPlan& hp, FFTPlanDev& pd) {
+// Device view of a convolution plan whose twiddles live in the image:
+// QPSTD_OK, QPSTD_ENOTSUP when a pass needs more threads per line than a CTA
+// holds (as qpstd_shot_create reports it), QPSTD_EINVAL when the twiddles do
+// not fit the static array.
+int put_plan(TableImage& im, const HostPlan& hp, FFTPlanDev& pd) {
+    int maxb = 1;
+    for (int r : hp.rad) maxb = std::max(maxb, hp.m / r);
+    if (maxb > QP_MAXTHREADS)
+        return fail(QPSTD_ENOTSUP, "transform needs more threads per line than a CTA holds");
     const float2* tw = put_complex(im, hp.w);
-    if (!tw) return false;
+    if (!tw) return fail(QPSTD_EINVAL, "tables exceed the static scratch");
     pd.n = hp.n;
     pd.m = hp.m;
     pd.blue = 0;
     pd.nst = (int)hp.rad.size();
-    int ns = 1, maxb = 1;
+    int ns = 1;
     for (int i = 0; i < pd.nst; i++) {
         FFTPass& q = pd.pass[i];
         q.R = hp.rad[i];
@@ -113,14 +121,12 @@ bool put_plan(TableImage& im, const HostPlan& hp, FFTPlanDev& pd) {
         q.B = hp.m / q.R;
         q.twstride = hp.m / (ns * q.R);
         q.ns_magic = (ns > 1) ? (unsigned)(((1ull << 32) + ns - 1) / ns) : 0u;
-        maxb = std::max(maxb, q.B);
         ns *= q.R;
     }
-    if (maxb > QP_MAXTHREADS) return false;
     pd.tx = (maxb + 31) / 32 * 32;
     pd.w = tw;
     pd.chirp = pd.bhat = nullptr;
-    return true;
+    return QPSTD_OK;
 }
 
 int lines_per_cta(int pairs, const FFTPlanDev& pd, size_t extra_per_line, size_t budget, bool pow2) {
@@ -185,7 +191,9 @@ extern "C" int qpstd_ac_advance_noalloc(const qpstd_shot_desc* d, const float* v
     if (build_conv_plan_host(nxx, cx) || build_conv_plan_host(nzz, cz))
         return fail(QPSTD_ENOTSUP, "no convolution plan for this length");
     FFTPlanDev px{}, pz{};
-    if (!put_plan(im, cx, px) || !put_plan(im, cz, pz)) return fail(QPSTD_EINVAL, "tables exceed the static scratch");
+    int prc = put_plan(im, cx, px);
+    if (prc == QPSTD_OK) prc = put_plan(im, cz, pz);
+    if (prc != QPSTD_OK) return prc;
     std::vector<std::complex<double>> H, T;
     const float2* tab[6];  // x velocity, x pressure, z velocity, z pressure derivatives; kx^2; kz^2
     for (int w = 0; w < 4; w++) {

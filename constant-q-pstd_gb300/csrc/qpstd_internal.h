@@ -49,6 +49,14 @@ struct FFTPlanDev {
     const float2* bhat;    // m values: DFT_m of the wrapped conj chirp, divided by m (Bluestein)
 };
 
+// Largest radix of a plan (host or device): kernels with plans up to radix 12
+// can run the 12-entry register array.
+__host__ __device__ inline int plan_max_radix(const FFTPlanDev& p) {
+    int r = 0;
+    for (int i = 0; i < p.nst; i++) r = (p.pass[i].R > r) ? p.pass[i].R : r;
+    return r;
+}
+
 // Receiver / source bookkeeping for one x-tile of columns.
 struct RecEntry {
     int gx, gz;   // padded-grid indices

@@ -355,8 +355,22 @@ int shot_create_ex(const qpstd_shot_desc* d, qpstd_shot** out, bool tune, qp::Ar
         qpstd_shot_destroy(s);
         return code;
     };
-    static int smem_ok = -1;
-    if (smem_ok != 0) smem_ok = (ac_set_smem_limits() || vz_set_smem_limits()) ? -1 : 0;
+    // the kernels' shared-memory limits are attributes of each device's context:
+    // raised once per device (the current one), under a lock
+    {
+        static std::mutex mu;
+        static bool raised[64] = {false};
+        int dev = 0;
+        cudaError_t de = cudaGetDevice(&dev);
+        if (de != cudaSuccess) return bail(cuda_fail(de, "cudaGetDevice"));
+        if (dev < 0 || dev >= 64) return bail(fail(QPSTD_ENOTSUP, "device index above 63"));
+        std::lock_guard<std::mutex> lk(mu);
+        if (!raised[dev]) {
+            if (ac_set_smem_limits() || vz_set_smem_limits())
+                return bail(fail(QPSTD_ECUDA, "cannot raise the shared-memory limit of the pass kernels"));
+            raised[dev] = true;
+        }
+    }
     s->nzh = nzz / 2 + 1;
     cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
@@ -691,14 +705,17 @@ static void vz_step(qpstd_shot* s, Wave& w, float src, int t_filter, float eta, 
     VxsArgs xs{};
     xs.nxx = nxx; xs.nzz = nzz; xs.nzh = nzh; xs.pl = s->px; xs.kx2 = s->kxsq; xs.kz2 = s->kzsq; xs.norm = norm;
     xs.plc = s->pxc;
-    // modes 0 and 1 (stationary symbols): per-kz convolution tables when built
+    // modes 0 and 1 (stationary symbols): per-kz convolution tables when built;
+    // launches on exact DFTs are timed as their own kind
     auto xspec = [&](VxsArgs& a) {
         if (s->xconv && a.mode != 2) {
             a.tab0 = s->xtab[a.mode == 0 ? 0 : 3];
             a.tab1 = s->xtab[1];
             a.tab2 = s->xtab[2];
+            ProfScope ps(s, QPSTD_K_XSPEC);
             launch_vz_xspec_conv(a, st);
         } else {
+            ProfScope ps(s, QPSTD_K_XSPEC_EXACT);
             launch_vz_xspec(a, st);
         }
     };
@@ -706,7 +723,6 @@ static void vz_step(qpstd_shot* s, Wave& w, float src, int t_filter, float eta, 
         VxsArgs a = xs;
         a.mode = 0; a.L = s->Lxs3;
         a.in = s->spec[0]; a.out0 = s->spec[1]; a.out1 = s->spec[2]; a.out2 = s->spec[3];
-        ProfScope ps(s, QPSTD_K_XSPEC);
         xspec(a);
     }
     {
@@ -722,7 +738,6 @@ static void vz_step(qpstd_shot* s, Wave& w, float src, int t_filter, float eta, 
         VxsArgs a = xs;
         a.mode = 1; a.L = s->Lxs;
         a.in = s->spec[0]; a.out0 = s->spec[1];
-        ProfScope ps(s, QPSTD_K_XSPEC);
         xspec(a);
     }
     {
@@ -757,7 +772,6 @@ static void vz_step(qpstd_shot* s, Wave& w, float src, int t_filter, float eta, 
             a.mode = 1;
         }
         if (a.mode == 2 && s->xconv) a.L = s->Lxs_exact;
-        ProfScope ps(s, QPSTD_K_XSPEC);
         xspec(a);
         w.aux_pending = true;
     }
@@ -1123,6 +1137,21 @@ extern "C" int qpstd_shot_advance(qpstd_shot* s, int t0, int nsteps, float* gath
 }
 
 extern "C" long long qpstd_shot_launch_count(const qpstd_shot* s) { return s ? s->launches : -1; }
+
+extern "C" long long qpstd_shot_info(const qpstd_shot* s, int key) {
+    if (!s) return -1;
+    switch (key) {
+        case QPSTD_INFO_X_CONV_M: return s->pxc.m;
+        case QPSTD_INFO_X_CONV_MAXRADIX: return plan_max_radix(s->pxc);
+        case QPSTD_INFO_X_EXACT_M: return s->px.m;
+        case QPSTD_INFO_X_EXACT_BLUE: return s->px.blue;
+        case QPSTD_INFO_X_SPEC_CONV: return s->xconv ? 1 : 0;
+        case QPSTD_INFO_Z_EXACT_M: return s->pz.m;
+        case QPSTD_INFO_Z_EXACT_MAXRADIX: return plan_max_radix(s->pz);
+        case QPSTD_INFO_Z_CONV_M: return s->pzc.m;
+        default: return -1;
+    }
+}
 
 extern "C" void* qpstd_shot_stream(qpstd_shot* s) { return s ? (void*)s->stream : nullptr; }
 

@@ -76,6 +76,7 @@ EXPORTS = {
     "qpstd_shot_pipeline_end": (C.c_int, [C.c_void_p]),
     "qpstd_shot_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "qpstd_shot_profile_read": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
+    "qpstd_shot_info": (C.c_longlong, [C.c_void_p, C.c_int]),
     "qpstd_batch_create": (C.c_int, [C.POINTER(ShotDesc), C.c_int, C.POINTER(C.c_void_p)]),
     "qpstd_batch_destroy": (C.c_int, [C.c_void_p]),
     "qpstd_batch_size": (C.c_int, [C.c_void_p]),
@@ -103,7 +104,10 @@ EXPORTS = {
     "qpstd_server_status": (C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "qpstd_server_wait": (C.c_int, [C.c_void_p, C.c_longlong]),
 }
-KIND_NAMES = ["xpass", "zpass", "xspec", "other", "plain"]
+KIND_NAMES = ["xpass", "zpass", "xspec", "other", "plain", "xspec_exact"]
+# keys of qpstd_shot_info
+INFO_KEYS = ["x_conv_m", "x_conv_maxradix", "x_exact_m", "x_exact_blue", "x_spec_conv", "z_exact_m",
+             "z_exact_maxradix", "z_conv_m"]
 
 
 def lib():
@@ -272,6 +276,10 @@ class Shot:
         cnt = (C.c_longlong * n)()
         _check(lib().qpstd_shot_profile_read(self.h, n, ms, cnt))
         return {KIND_NAMES[k]: (ms[k], cnt[k]) for k in range(n)}
+
+    def info(self) -> dict:
+        """The transforms this shot runs (qpstd_shot_info)."""
+        return {k: int(lib().qpstd_shot_info(self.h, i)) for i, k in enumerate(INFO_KEYS)}
 
 
 class Batch:

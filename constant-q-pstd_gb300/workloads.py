@@ -207,3 +207,50 @@ def make_shot(kind: int, nx_model: int, nz_model: int, pml: int, nt: int, dt: fl
     if visco:
         d["taoc"] = float(win["tao"].max())
     return d
+
+
+def qrtm4_shots(nt: int = 5000, snaps: int = 30, n: int = 64, seed: int = 1004, kind: int = 3):
+    """The batched Q-RTM workload: n shots with uneven windows, nx ~ U(600, 2000)
+    columns at a random offset of a seeded 600 (z) x 6000 (x) parent model, CPML
+    30, dt 0.5 ms, fd 20 Hz, the source at the window centre and a receiver in
+    every window column at z = 2 cells.  The draws do not depend on nt or snaps,
+    so a shortened run of shot i has shot i's window."""
+    rng = np.random.default_rng(seed)
+    parent = parent_model(6000, 600, seed, nlayers=12, nanom=3)
+    shots = []
+    for _ in range(n):
+        nx = int(rng.integers(600, 2001))
+        x0 = int(rng.integers(0, 6000 - nx + 1))
+        shots.append(window_of_parent(kind, parent, x0, nx, 30, nt, 0.0005, 20.0, snaps))
+    return shots
+
+
+def artm3_shots(nt: int = 6000, snaps: int = 40, seed: int = 1003):
+    """The large acoustic RTM shot: 800 (z) x 2400 (x) model, 12 seeded layers and 3
+    anomalies, CPML 30, dt 0.5 ms.  Returns (migration shot on the 8-cell Gaussian
+    blurred model, the same shot on the unblurred model that makes the observed
+    data)."""
+    mig = make_shot(2, 2400, 800, 30, nt, 0.0005, 20.0, seed=seed, nlayers=12, nanom=3,
+                    smooth_cells=8.0, snaps=snaps)
+    true = make_shot(0, 2400, 800, 30, nt, 0.0005, 20.0, seed=seed, nlayers=12, nanom=3)
+    return mig, true
+
+
+def synthetic_obs(d: dict, seed: int) -> np.ndarray:
+    """Observed data with the shape of a Q-RTM gather (nt x nr): a few
+    hyperbolic reflections of the source wavelet.  The cost of RTM does not
+    depend on the values, so the batch does not need 64 modeling runs."""
+    rng = np.random.default_rng(seed)
+    nt, nr, dt = d["nt"], len(d["gxg"]), d["dt"]
+    w = ricker(nt, dt, d["fd"])
+    off = (np.asarray(d["gxg"]) - d["xsg"]) * d["dx"]
+    obs = np.zeros((nt, nr))
+    t = np.arange(nt) * dt
+    for _ in range(4):
+        t0, v = rng.uniform(0.2, 1.8), rng.uniform(1800.0, 4000.0)
+        tr = np.sqrt(t0 ** 2 + (off / v) ** 2)
+        idx = np.clip(np.rint(tr / dt).astype(int), 0, nt - 1)
+        for j in range(nr):
+            k = idx[j]
+            obs[k:, j] += rng.uniform(-1, 1) * w[: nt - k]
+    return obs.astype(np.float32)

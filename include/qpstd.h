@@ -135,9 +135,23 @@ void *qpstd_shot_stream(qpstd_shot *s);
 #define QPSTD_K_XSPEC 2   /* x-line pass over z-spectra (2-D isotropic operators) */
 #define QPSTD_K_OTHER 3   /* small helpers (checkpoint-0 source sample, filters) */
 #define QPSTD_K_PLAIN 4   /* one whole plain-form step (cuFFT calls + elementwise kernels) */
-#define QPSTD_NKINDS 5
+#define QPSTD_K_XSPEC_EXACT 5 /* x-line pass over z-spectra on exact DFTs (Bluestein when nxx needs it) */
+#define QPSTD_NKINDS 6
 int qpstd_shot_set_profiling(qpstd_shot *s, int on);
 int qpstd_shot_profile_read(qpstd_shot *s, int nkinds, double *ms, long long *count);
+
+/* Facts about the transforms a created shot runs (for tests and tools); -1
+ * for a null shot or an unknown key.  No counterpart in the reference, whose
+ * cufftPlan2d chooses its own algorithm. */
+#define QPSTD_INFO_X_CONV_M 0        /* length of the x convolution transform (separable operators) */
+#define QPSTD_INFO_X_CONV_MAXRADIX 1 /* largest radix of that transform */
+#define QPSTD_INFO_X_EXACT_M 2       /* inner length of the exact length-nxx DFT (Bluestein: >= 2nxx-1) */
+#define QPSTD_INFO_X_EXACT_BLUE 3    /* 1 if the exact x DFT runs through Bluestein's identity */
+#define QPSTD_INFO_X_SPEC_CONV 4     /* 1 if stationary 2-D symbols run as per-kz x convolutions */
+#define QPSTD_INFO_Z_EXACT_M 5       /* inner length of the exact length-nzz DFT */
+#define QPSTD_INFO_Z_EXACT_MAXRADIX 6
+#define QPSTD_INFO_Z_CONV_M 7
+long long qpstd_shot_info(const qpstd_shot *s, int key);
 
 /* ---- batches: many resident shots advancing together ---------------------
  * The reference runs a rank's shots one after another (the shot loop of
@@ -226,10 +240,10 @@ int qpstd_lowrank_apply_device(qpstd_lowrank *h, const float *d_in, float *d_out
 
 /* ---- acoustic steps without device allocation ---------------------------
  * No counterpart in the reference (its acforward allocates all device memory
- * itself).  For callers that cannot call cudaMalloc -- code running while
- * another part of the process captures a CUDA graph, plug-ins that may only
- * use the buffers their host hands them, hosts whose device memory belongs to
- * a pool they do not own.  Runs nsteps acoustic steps (aps / the source side of
+ * itself).  For callers that cannot call cudaMalloc -- plug-ins that may only
+ * use the buffers their host application hands them, hosts whose device memory
+ * all belongs to a pool they do not own, latency-critical callers that may not
+ * allocate (cudaFree synchronises the device).  Runs nsteps acoustic steps (aps / the source side of
  * artm) from step index t0, exactly as qpstd_shot_advance does, with every
  * scratch buffer and table in a static array of QPSTD_NOALLOC_FLOATS floats
  * (24 MiB) that each GPU loading the library keeps until exit; grids above

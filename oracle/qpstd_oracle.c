@@ -650,8 +650,12 @@ static void step_source(ctx_t *c, double *st, int t, double *ssg, int restart) {
 /* Drivers                                                                   */
 /* ======================================================================== */
 
+/* Source-side steps.  For artm / qrtm these are the steps of the first forward
+ * sweep (the advance branch, sgpstd-qrtm/acsglw.cu:508-512), the Q-RTM aux filter at time index t
+ * with eta = etas; illumination is not accumulated here. */
 int orc_model_steps(const orc_shot *s, double *st, int t0, int nsteps, double *gather) {
-    if (s->kind != ORC_APS && s->kind != ORC_VAPS) return -1;
+    if (s->kind < ORC_APS || s->kind > ORC_QRTM) return -1;
+    const double eta = (s->kind == ORC_QRTM) ? s->etas : 0.0;
     ctx_t c;
     ctx_init(&c, s);
     for (int t = t0; t < t0 + nsteps; t++) {
@@ -661,7 +665,7 @@ int orc_model_steps(const orc_shot *s, double *st, int t0, int nsteps, double *g
             for (int i = 0; i < s->nr; i++)
                 gather[(size_t)(t - t0) * s->nr + i] = p[(size_t)s->gxg[i] * s->nzz + s->gzg[i]];
         }
-        stage_grad(&c, st, t, 0.0, t);
+        stage_grad(&c, st, t, eta, t);
     }
     ctx_free(&c);
     return 0;
