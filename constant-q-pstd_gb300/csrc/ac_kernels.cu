@@ -23,8 +23,8 @@ namespace qp {
 
 // ---- z pass ----------------------------------------------------------------
 // staged fields (each L*2*nzz floats): 0 vz, 1 psi_pz, 2 bbz, 3 psi_vz, 4 Dx
-template <int RMAX>
-__global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) ac_zpass_kernel(AcZArgs a) {
+template <class FP>
+__global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) ac_zpass_kernel(AcZArgs a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
     const FFTCtx fc = make_ctx(a.pl, s_pass);
@@ -66,7 +66,7 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) ac_zpass_ke
     if (a.do_v) {
         zload_pair(a.p, line, nzz, has0, has1, r0, r1);
         __syncthreads();
-        roundtrip_conv<RMAX>(smem, ld, fc, L, a.HzP);
+        roundtrip_conv<FP>(smem, ld, fc, L, a.HzP);
         if (a.stage) cp_async_wait_all();
         for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
             const float2 d = line[k];
@@ -91,7 +91,7 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) ac_zpass_ke
     }
     if (!a.do_div) return;
     __syncthreads();
-    roundtrip_conv<RMAX>(smem, ld, fc, L, a.HzM);
+    roundtrip_conv<FP>(smem, ld, fc, L, a.HzM);
     if (a.stage) cp_async_wait_all();
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 d = line[k];
@@ -112,7 +112,7 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) ac_zpass_ke
         line[k] = dv;
     }
     __syncthreads();
-    roundtrip_conv<RMAX>(smem, ld, fc, L, a.kz2);
+    roundtrip_conv<FP>(smem, ld, fc, L, a.kz2);
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 d = line[k];
         if (has0) a.Lz[r0 + k] = d.x;
@@ -126,8 +126,8 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) ac_zpass_ke
 // first transform (p, or vx) is its own cp.async group, so the transform starts
 // while the epilogue inputs are still arriving.
 // P: this launch does the p update (a.do_p); RMAX: largest radix of the plan (12 or 16)
-template <bool P, int RMAX>
-__global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) ac_xpass_kernel(AcXArgs a) {
+template <bool P, class FP>
+__global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) ac_xpass_kernel(AcXArgs a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
     const FFTCtx fc = make_ctx(a.pl, s_pass);
@@ -184,7 +184,7 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) ac_xpass_ke
             if (a.stage) S(0, g) = v;
         }
         __syncthreads();
-        roundtrip_conv<RMAX>(smem, ld, fc, L, a.kx2);
+        roundtrip_conv<FP>(smem, ld, fc, L, a.kx2);
         if (a.stage) cp_async_wait_all();
         for (int g = T.t0; g < T.tot; g += T.nthr) {
             int c, ix;
@@ -244,7 +244,7 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) ac_xpass_ke
             }
         }
         __syncthreads();
-        roundtrip_conv<RMAX>(smem, ld, fc, L, a.HxP);
+        roundtrip_conv<FP>(smem, ld, fc, L, a.HxP);
         if (a.stage) cp_async_wait_all();
         for (int g = T.t0; g < T.tot; g += T.nthr) {
             int c, ix;
@@ -283,7 +283,7 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) ac_xpass_ke
             }
         }
         __syncthreads();
-        roundtrip_conv<RMAX>(smem, ld, fc, L, a.HxM);
+        roundtrip_conv<FP>(smem, ld, fc, L, a.HxM);
         if (a.stage) cp_async_wait_all();
         for (int g = T.t0; g < T.tot; g += T.nthr) {
             int c, ix;
@@ -307,11 +307,18 @@ size_t ac_xpass_smem(int L, int m, int nxx, int nstaged) {
     return sizeof(float2) * (size_t)L * m + sizeof(float) * (size_t)nstaged * nxx * 2 * L;
 }
 
+// Plans compiled into the acoustic z pass (its convolution plan): 1728 = 12^3
+// (nz 800 + CPML 30: 860 needs the convolution length), 660, 200 (see ZPlans
+// in vz_kernels.cu).
+using AcZPlans = PlanList<CtFFT<12, 12, 12>, CtFFT<11, 10, 6>, CtFFT<5, 5, 8>>;
+
 void launch_ac_zpass(const AcZArgs& a, cudaStream_t s) {
     const int grid = (a.nxx + 2 * a.L - 1) / (2 * a.L);
     const size_t sm = ac_zpass_smem(a.L, a.pl.m, a.nzz, a.stage);
-    if (plan_max_radix(a.pl) <= 12) ac_zpass_kernel<12><<<grid, dim3(a.pl.tx, a.L), sm, s>>>(a);
-    else ac_zpass_kernel<16><<<grid, dim3(a.pl.tx, a.L), sm, s>>>(a);
+    const dim3 blk(a.pl.tx, a.L);
+#define L_(FPT) ac_zpass_kernel<FPT><<<grid, blk, sm, s>>>(a)
+    QP_DISPATCH(AcZPlans, a.pl, NoExtraPlan{}, plan_max_radix(a.pl) <= 12, L_);
+#undef L_
 }
 
 void launch_ac_xpass(const AcXArgs& a, cudaStream_t s) {
@@ -321,21 +328,32 @@ void launch_ac_xpass(const AcXArgs& a, cudaStream_t s) {
     // the instance without the p update carries only the transforms it runs
     const dim3 blk(a.pl.tx, a.L);
     const bool r12 = plan_max_radix(a.pl) <= 12;
-    if (a.do_p && r12) ac_xpass_kernel<true, 12><<<grid, blk, sm, s>>>(a);
-    else if (a.do_p) ac_xpass_kernel<true, 16><<<grid, blk, sm, s>>>(a);
-    else if (r12) ac_xpass_kernel<false, 12><<<grid, blk, sm, s>>>(a);
-    else ac_xpass_kernel<false, 16><<<grid, blk, sm, s>>>(a);
+    if (a.do_p && r12) ac_xpass_kernel<true, RtFFT<12>><<<grid, blk, sm, s>>>(a);
+    else if (a.do_p) ac_xpass_kernel<true, RtFFT<16>><<<grid, blk, sm, s>>>(a);
+    else if (r12) ac_xpass_kernel<false, RtFFT<12>><<<grid, blk, sm, s>>>(a);
+    else ac_xpass_kernel<false, RtFFT<16>><<<grid, blk, sm, s>>>(a);
 }
 
 int ac_set_smem_limits() {
     const int lim = QP_SMEM_DYN_MAX;
-    cudaError_t e1 = cudaFuncSetAttribute(ac_zpass_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-    if (e1 == cudaSuccess) e1 = cudaFuncSetAttribute(ac_zpass_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-    cudaError_t e2 = cudaFuncSetAttribute(ac_xpass_kernel<true, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-    if (e2 == cudaSuccess) e2 = cudaFuncSetAttribute(ac_xpass_kernel<true, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-    cudaError_t e3 = cudaFuncSetAttribute(ac_xpass_kernel<false, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-    if (e3 == cudaSuccess) e3 = cudaFuncSetAttribute(ac_xpass_kernel<false, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-    return (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess) ? 0 : -1;
+    int bad = 0;
+    auto z = [&](auto fp) {
+        bad |= cudaFuncSetAttribute(ac_zpass_kernel<decltype(fp)>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) !=
+               cudaSuccess;
+    };
+    z(RtFFT<12>{});
+    z(RtFFT<16>{});
+    for_each_plan(AcZPlans{}, z);
+    auto x = [&](auto fp) {
+        using F = decltype(fp);
+        bad |= cudaFuncSetAttribute(ac_xpass_kernel<true, F>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) !=
+               cudaSuccess;
+        bad |= cudaFuncSetAttribute(ac_xpass_kernel<false, F>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) !=
+               cudaSuccess;
+    };
+    x(RtFFT<12>{});
+    x(RtFFT<16>{});
+    return bad ? -1 : 0;
 }
 
 }  // namespace qp

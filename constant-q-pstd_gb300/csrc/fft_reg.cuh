@@ -273,15 +273,139 @@ __device__ __forceinline__ FFTCtx make_ctx(const FFTPlanDev& pl, FFTPass* s_pass
     return c;
 }
 
-template <int S, int RMAX = 16> __device__ __forceinline__ void fft_m(float2* buf, int ld, const FFTCtx& pl, int L) {
-    fft_m_impl<S, RMAX>(buf, ld, pl.sp, pl.nst, pl.w, L);
+// ---- transform policies ---------------------------------------------------------
+// A pass kernel is compiled for one policy, the way it runs its length-m
+// transforms:
+//   RtFFT<RMAX>  the plan's radices read at run time (any plan the host builds;
+//                one RMAX-entry register array and a radix switch per pass);
+//   CtFFT<Rs...> one plan compiled in, radices Rs in pass order: register
+//                arrays of the exact radix, constant strides, divisors and
+//                twiddle strides, and no switch, so each pass is straight-line
+//                code of its own radix.  The launchers use it when the shot's
+//                plan is one of the compiled ones (the lengths the benchmark
+//                workloads and the convolution-length ladder produce).
+// Both compute the same Stockham passes with the same twiddles, so their
+// results agree to the last bit of the arithmetic order.
+template <int RMAX> struct RtFFT {
+    static constexpr int kMaxRadix = RMAX;
+    template <int S> __device__ __forceinline__ static void run(float2* buf, int ld, const FFTCtx& c, int L) {
+        fft_m_impl<S, RMAX>(buf, ld, c.sp, c.nst, c.w, L);
+    }
+};
+
+// Compile-time Stockham passes (NS = product of the earlier radices).
+template <int S, int M, int NS, int R, int... Rest>
+__device__ __forceinline__ void ct_passes(float2* line, const float2* __restrict__ tw, bool lact) {
+    constexpr int B = M / R;
+    const int j = threadIdx.x;
+    const bool act = lact && (j < B);
+    float2 v[R];
+    int k = 0;
+    if (act) {
+        if constexpr (NS > 1) k = j % NS;
+#pragma unroll
+        for (int r = 0; r < R; r++) v[r] = line[j + r * B];
+        if constexpr (NS > 1) {
+            float2 w1 = __ldg(&tw[k * (M / (NS * R))]);
+            if (S > 0) w1.y = -w1.y;
+            float2 w = w1;
+#pragma unroll
+            for (int r = 1; r < R; r++) {
+                v[r] = cmul(v[r], w);
+                w = cmul(w, w1);
+            }
+        }
+        dft<R, S>(v);
+    }
+    __syncthreads();
+    if (act) {
+        const int base = (j - k) * R + k;
+#pragma unroll
+        for (int r = 0; r < R; r++) line[base + r * NS] = v[r];
+    }
+    __syncthreads();
+    if constexpr (sizeof...(Rest) > 0) ct_passes<S, M, NS * R, Rest...>(line, tw, lact);
+}
+
+template <int... Rs> struct CtFFT {
+    static constexpr int kNst = sizeof...(Rs);
+    static constexpr int kRad[kNst] = {Rs...};
+    static constexpr int M = (Rs * ...);
+    static constexpr int kMaxRadix = [] {
+        int r = 0;
+        for (int x : {Rs...}) r = x > r ? x : r;
+        return r;
+    }();
+    template <int S> __device__ __forceinline__ static void run(float2* buf, int ld, const FFTCtx& c, int L) {
+        ct_passes<S, M, 1, Rs...>(buf + threadIdx.y * ld, c.w, threadIdx.y < L);
+    }
+    // host: is p exactly this plan?
+    static bool matches(const FFTPlanDev& p) {
+        if (p.m != M || p.nst != kNst) return false;
+        for (int i = 0; i < kNst; i++)
+            if (p.pass[i].R != kRad[i]) return false;
+        return true;
+    }
+};
+
+// A list of compiled plans and its dispatch: first_match calls fn(Policy{})
+// with the first listed plan that p equals and returns true, else false.
+template <class... Ps> struct PlanList {};
+template <class Fn> bool first_match(PlanList<>, const FFTPlanDev&, Fn&&) { return false; }
+template <class P0, class... Ps, class Fn> bool first_match(PlanList<P0, Ps...>, const FFTPlanDev& p, Fn&& fn) {
+    if (P0::matches(p)) {
+        fn(P0{});
+        return true;
+    }
+    return first_match(PlanList<Ps...>{}, p, fn);
+}
+// fn(Policy{}) for every plan of the list (e.g. to set kernel attributes)
+template <class Fn> void for_each_plan(PlanList<>, Fn&&) {}
+template <class P0, class... Ps, class Fn> void for_each_plan(PlanList<P0, Ps...>, Fn&& fn) {
+    fn(P0{});
+    for_each_plan(PlanList<Ps...>{}, fn);
+}
+
+// Launches kernel template K for plan p: a compiled plan when p is one (and
+// every extra plan of the kernel equals it), else the run-time plan.
+#define QP_DISPATCH(LIST, p, same_extra, r12, LAUNCH)                                  \
+    do {                                                                              \
+        const bool ct_ = first_match(LIST{}, p, [&](auto fp_) {                        \
+            using FPc = decltype(fp_);                                                \
+            if (same_extra(FPc{})) {                                                  \
+                LAUNCH(FPc);                                                          \
+            } else if (r12) {                                                         \
+                LAUNCH(RtFFT<12>);                                                    \
+            } else {                                                                  \
+                LAUNCH(RtFFT<16>);                                                    \
+            }                                                                         \
+        });                                                                           \
+        if (!ct_) {                                                                   \
+            if (r12) {                                                                \
+                LAUNCH(RtFFT<12>);                                                    \
+            } else {                                                                  \
+                LAUNCH(RtFFT<16>);                                                    \
+            }                                                                         \
+        }                                                                             \
+    } while (0)
+
+// QP_DISPATCH's same_extra for kernels with one plan
+struct NoExtraPlan {
+    template <class F> bool operator()(F) const { return true; }
+};
+
+// FP: the transform policy (RtFFT / CtFFT above)
+template <int S, class FP = RtFFT<16>>
+__device__ __forceinline__ void fft_m(float2* buf, int ld, const FFTCtx& pl, int L) {
+    FP::template run<S>(buf, ld, pl, L);
 }
 
 // Exact length-n DFT of entries [0,n) of each line, in place.  Caller has
 // synchronised after filling buf; ends with a barrier.
-template <int S, int RMAX = 16> __device__ __forceinline__ void dft_n(float2* buf, int ld, const FFTCtx& pl, int L) {
+template <int S, class FP = RtFFT<16>>
+__device__ __forceinline__ void dft_n(float2* buf, int ld, const FFTCtx& pl, int L) {
     if (!pl.blue) {
-        fft_m<S, RMAX>(buf, ld, pl, L);
+        fft_m<S, FP>(buf, ld, pl, L);
         return;
     }
     const int n = pl.n, m = pl.m;
@@ -300,11 +424,11 @@ template <int S, int RMAX = 16> __device__ __forceinline__ void dft_n(float2* bu
             line[k] = v;
         }
     __syncthreads();
-    fft_m<-1, RMAX>(buf, ld, pl, L);
+    fft_m<-1, FP>(buf, ld, pl, L);
     if (act)
         for (int k = threadIdx.x; k < m; k += blockDim.x) line[k] = cmul(line[k], __ldg(&pl.bhat[k]));
     __syncthreads();
-    fft_m<+1, RMAX>(buf, ld, pl, L);
+    fft_m<+1, FP>(buf, ld, pl, L);
     if (act)
         for (int k = threadIdx.x; k < n; k += blockDim.x) {
             float2 y = cmul(line[k], __ldg(&pl.chirp[k]));
@@ -318,7 +442,7 @@ template <int S, int RMAX = 16> __device__ __forceinline__ void dft_n(float2* bu
 // plan: y[0,n) = IFFT_m(Hm .* FFT_m(x zero-padded to m)), Hm from conv_table
 // (m = n when n itself is smooth).  Caller has synchronised after filling
 // entries [0,n); ends with a barrier.
-template <int RMAX = 16>
+template <class FP = RtFFT<16>>
 __device__ __forceinline__ void roundtrip_conv(float2* buf, int ld, const FFTCtx& pl, int L,
                                                const float2* __restrict__ Hm) {
     const int l = threadIdx.y;
@@ -329,11 +453,11 @@ __device__ __forceinline__ void roundtrip_conv(float2* buf, int ld, const FFTCtx
             for (int k = pl.n + threadIdx.x; k < pl.m; k += blockDim.x) line[k] = make_float2(0.f, 0.f);
         __syncthreads();
     }
-    fft_m<-1, RMAX>(buf, ld, pl, L);
+    fft_m<-1, FP>(buf, ld, pl, L);
     if (act)
         for (int k = threadIdx.x; k < pl.m; k += blockDim.x) line[k] = cmul(line[k], __ldg(&Hm[k]));
     __syncthreads();
-    fft_m<+1, RMAX>(buf, ld, pl, L);
+    fft_m<+1, FP>(buf, ld, pl, L);
 }
 
 // y = IDFT(H .* DFT(x)) with a complex symbol (length n, 1/n folded in).

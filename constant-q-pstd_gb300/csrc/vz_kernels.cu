@@ -34,8 +34,8 @@ namespace qp {
     (void)r1;
 
 // ---- z pass A ---------------------------------------------------------------
-template <int RMAX>
-__global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passA_kernel(VzArgsA a) {
+template <class FP>
+__global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passA_kernel(VzArgsA a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
     __shared__ FFTPass s_pass_c[QP_MAXST];
@@ -50,7 +50,7 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passA_ke
     if (a.aux_spec) {
         zrepack(a.aux_spec, line, nzz, nzh, has0, has1, xa);
         __syncthreads();
-        dft_n<+1, RMAX>(smem, ld, fc, L);
+        dft_n<+1, FP>(smem, ld, fc, L);
         for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
             const float2 v = line[k];
             if (has0) a.aux[r0 + k] = v.x;
@@ -60,7 +60,7 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passA_ke
     }
     zload_pair(a.vz, line, nzz, has0, has1, r0, r1);
     __syncthreads();
-    roundtrip_conv<RMAX>(smem, ld, fcc, L, a.HzM);
+    roundtrip_conv<FP>(smem, ld, fcc, L, a.HzM);
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 d = line[k];
         const float ib = a.i_bz[k], ia = a.i_az[k];
@@ -80,7 +80,7 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passA_ke
         line[k] = dv;
     }
     __syncthreads();
-    dft_n<-1, RMAX>(smem, ld, fc, L);
+    dft_n<-1, FP>(smem, ld, fc, L);
     zunpack(line, a.G, nzz, nzh, has0, has1, xa);
 }
 
@@ -99,9 +99,9 @@ __device__ __forceinline__ float spec_symbol(const VxsArgs& a, int j, float k2) 
     return ka - num / den;
 }
 
-// RMAX: largest radix of the exact plan (12 or 16; Bluestein plans included).
-template <int RMAX>
-__global__ void __maxnreg__(RMAX == 12 ? QP_PASS_REGS : QP_EXACT_REGS) vz_xspec_kernel(VxsArgs a) {
+// FP: transform policy of the exact plan (Bluestein plans included).
+template <class FP>
+__global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_PASS_REGS : QP_EXACT_REGS) vz_xspec_kernel(VxsArgs a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
     const FFTCtx fc = make_ctx(a.pl, s_pass);
@@ -119,7 +119,7 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_PASS_REGS : QP_EXACT_REGS) vz_xspec_
         smem[c * ld + ix] = (kz < nzh) ? a.in[(size_t)ix * nzh + kz] : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    dft_n<-1, RMAX>(smem, ld, fc, L);
+    dft_n<-1, FP>(smem, ld, fc, L);
     if (nout == 3) {
         for (int ix = threadIdx.x; ix < nxx; ix += blockDim.x) X[threadIdx.y * ld + ix] = line[ix];
         __syncthreads();
@@ -139,7 +139,7 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_PASS_REGS : QP_EXACT_REGS) vz_xspec_
                 ln[ix] = cscale(src[ix], spec_symbol(a, j, a.kx2[ix] + kzsq) * a.norm);
         }
         __syncthreads();
-        dft_n<+1, RMAX>(smem, ld, fc, L);
+        dft_n<+1, FP>(smem, ld, fc, L);
         const int lgl = 31 - __clz(L), kzb = blockIdx.x * L, tl = L * nxx;
         for (int g = threadIdx.y * blockDim.x + threadIdx.x; g < tl; g += blockDim.x * blockDim.y) {
             const int c = g & (L - 1), ix = g >> lgl;
@@ -160,9 +160,9 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_PASS_REGS : QP_EXACT_REGS) vz_xspec_
 // replaces the exact (Bluestein) DFTs: one forward transform, then per output a
 // multiply by the column's table and one inverse transform.
 // NOUT = 3 (mode 0) or 1 (mode 1): each instance carries only the transforms it runs.
-// RMAX: largest radix of the convolution plan (12 or 16).
-template <int NOUT, int RMAX>
-__global__ void __maxnreg__(NOUT == 3 ? QP_WIDE_REGS : RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS)
+// FP: transform policy of the convolution plan.
+template <int NOUT, class FP>
+__global__ void __maxnreg__(NOUT == 3 ? QP_WIDE_REGS : FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS)
     vz_xspec_conv_kernel(VxsArgs a) {
     extern __shared__ float2 smem[];
     __shared__ FFTPass s_pass[QP_MAXST];
@@ -182,7 +182,7 @@ __global__ void __maxnreg__(NOUT == 3 ? QP_WIDE_REGS : RMAX == 12 ? QP_R12_REGS 
     }
     for (int k = nxx + threadIdx.x; k < m; k += blockDim.x) line[k] = make_float2(0.f, 0.f);
     __syncthreads();
-    fft_m<-1, RMAX>(smem, ld, fc, L);
+    fft_m<-1, FP>(smem, ld, fc, L);
     const int kz = min(kz0 + (int)threadIdx.y, nzh - 1);
     if (nout == 3) {
         for (int k = threadIdx.x; k < m; k += blockDim.x) X[threadIdx.y * ld + k] = line[k];
@@ -195,7 +195,7 @@ __global__ void __maxnreg__(NOUT == 3 ? QP_WIDE_REGS : RMAX == 12 ? QP_R12_REGS 
         const float* tk = tab + (size_t)kz * mh;
         for (int k = threadIdx.x; k < m; k += blockDim.x) line[k] = cscale(src[k], __ldg(&tk[min(k, m - k)]));
         __syncthreads();
-        fft_m<+1, RMAX>(smem, ld, fc, L);
+        fft_m<+1, FP>(smem, ld, fc, L);
         for (int g = t0; g < tot; g += nthr) {
             const int c = g & (L - 1), ix = g >> lg;
             if (kz0 + c < nzh) out[(size_t)ix * nzh + kz0 + c] = smem[c * ld + ix];
@@ -249,8 +249,8 @@ __global__ void __launch_bounds__(768, 1) vz_convtab_kernel(VtabArgs a) {
 }
 
 // ---- z pass B -----------------------------------------------------------------
-template <int RMAX>
-__global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passB_kernel(VzArgsB a) {
+template <class FP>
+__global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passB_kernel(VzArgsB a) {
     ZPASS_SETUP
     const int nzh = a.nzh;
     float2* acc = smem + (size_t)(L + threadIdx.y) * ld;  // running total of this line pair
@@ -258,7 +258,7 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passB_ke
     auto term = [&](const float2* spec, const float* cf, float sg, bool first) {
         zrepack(spec, line, nzz, nzh, has0, has1, xa);
         __syncthreads();
-        dft_n<+1, RMAX>(smem, ld, fc, L);
+        dft_n<+1, FP>(smem, ld, fc, L);
         for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
             const float2 y = line[k];
             float2 t = first ? make_float2(0.f, 0.f) : acc[k];
@@ -285,18 +285,18 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passB_ke
         line[k] = v;
     }
     __syncthreads();
-    dft_n<-1, RMAX>(smem, ld, fc, L);
+    dft_n<-1, FP>(smem, ld, fc, L);
     zunpack(line, a.T, nzz, nzh, has0, has1, xa);
 }
 
 // ---- z pass C -----------------------------------------------------------------
-template <int RMAX>
-__global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passC_kernel(VzArgsC a) {
+template <class FP>
+__global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passC_kernel(VzArgsC a) {
     ZPASS_SETUP
     const int nzh = a.nzh;
     zrepack(a.Dspec, line, nzz, nzh, has0, has1, xa);
     __syncthreads();
-    dft_n<+1, RMAX>(smem, ld, fc, L);
+    dft_n<+1, FP>(smem, ld, fc, L);
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 D = line[k];
         float2 pn = make_float2(0.f, 0.f);
@@ -346,12 +346,12 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passC_ke
     __syncthreads();
     // forward z transform of the new p: half spectrum for the aux operator and
     // the staggered z derivative from the same transform
-    dft_n<-1, RMAX>(smem, ld, fc, L);
+    dft_n<-1, FP>(smem, ld, fc, L);
     zunpack(line, a.P, nzz, nzh, has0, has1, xa);
     __syncthreads();
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) line[k] = cmul(line[k], __ldg(&a.HzP[k]));
     __syncthreads();
-    dft_n<+1, RMAX>(smem, ld, fc, L);
+    dft_n<+1, FP>(smem, ld, fc, L);
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 d = line[k];
         const float hb = a.h_bz[k], ha = a.h_az[k];
@@ -371,12 +371,12 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passC_ke
 }
 
 // ---- z inverse only -------------------------------------------------------------
-template <int RMAX>
-__global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) vz_zinv_kernel(VzArgsI a) {
+template <class FP>
+__global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz_zinv_kernel(VzArgsI a) {
     ZPASS_SETUP
     zrepack(a.spec, line, nzz, a.nzh, has0, has1, xa);
     __syncthreads();
-    dft_n<+1, RMAX>(smem, ld, fc, L);
+    dft_n<+1, FP>(smem, ld, fc, L);
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 v = line[k];
         if (has0) a.out[r0 + k] = v.x;
@@ -388,63 +388,82 @@ __global__ void __maxnreg__(RMAX == 12 ? QP_R12_REGS : QP_PASS_REGS) vz_zinv_ker
 static size_t lsm(int L, int m, int nbuf) { return sizeof(float2) * (size_t)nbuf * L * m; }
 static int zgrid(int nxx, int L) { return (nxx + 2 * L - 1) / (2 * L); }
 
+// Plans compiled into the z passes (CtFFT): 660 = 11*10*6 (the Q-RTM batch's
+// nz 600 + CPML 30), 200 = 5*5*8 (nz 160 + CPML 20).  Other lengths run the
+// run-time plan (RtFFT, 12- or 16-entry register array).
+using ZPlans = PlanList<CtFFT<11, 10, 6>, CtFFT<5, 5, 8>>;
+
+
 void launch_vz_passA(const VzArgsA& a, cudaStream_t s) {
     const dim3 blk(max(a.pl.tx, a.plc.tx), a.L);
     const size_t sm = lsm(a.L, max(a.pl.m, a.plc.m), 1);
-    if (plan_max_radix(a.pl) <= 12 && plan_max_radix(a.plc) <= 12) vz_passA_kernel<12><<<zgrid(a.nxx, a.L), blk, sm, s>>>(a);
-    else vz_passA_kernel<16><<<zgrid(a.nxx, a.L), blk, sm, s>>>(a);
+    const bool r12 = plan_max_radix(a.pl) <= 12 && plan_max_radix(a.plc) <= 12;
+    auto same_plc = [&](auto fp) { return decltype(fp)::matches(a.plc); };
+#define L_(FPT) vz_passA_kernel<FPT><<<zgrid(a.nxx, a.L), blk, sm, s>>>(a)
+    QP_DISPATCH(ZPlans, a.pl, same_plc, r12, L_);
+#undef L_
 }
 void launch_vz_xspec(const VxsArgs& a, cudaStream_t s) {
     const int grid = (a.nzh + a.L - 1) / a.L;
     const size_t sm = lsm(a.L, a.pl.m, a.mode == 0 ? 2 : 1);
-    if (plan_max_radix(a.pl) <= 12) vz_xspec_kernel<12><<<grid, dim3(a.pl.tx, a.L), sm, s>>>(a);
-    else vz_xspec_kernel<16><<<grid, dim3(a.pl.tx, a.L), sm, s>>>(a);
+    if (plan_max_radix(a.pl) <= 12) vz_xspec_kernel<RtFFT<12>><<<grid, dim3(a.pl.tx, a.L), sm, s>>>(a);
+    else vz_xspec_kernel<RtFFT<16>><<<grid, dim3(a.pl.tx, a.L), sm, s>>>(a);
 }
 void launch_vz_xspec_conv(const VxsArgs& a, cudaStream_t s) {
     const int grid = (a.nzh + a.L - 1) / a.L;
     const dim3 blk(a.plc.tx, a.L);
     const bool r12 = plan_max_radix(a.plc) <= 12;
-    if (a.mode == 0 && r12) vz_xspec_conv_kernel<3, 12><<<grid, blk, lsm(a.L, a.plc.m, 2), s>>>(a);
-    else if (a.mode == 0) vz_xspec_conv_kernel<3, 16><<<grid, blk, lsm(a.L, a.plc.m, 2), s>>>(a);
-    else if (r12) vz_xspec_conv_kernel<1, 12><<<grid, blk, lsm(a.L, a.plc.m, 1), s>>>(a);
-    else vz_xspec_conv_kernel<1, 16><<<grid, blk, lsm(a.L, a.plc.m, 1), s>>>(a);
+    if (a.mode == 0 && r12) vz_xspec_conv_kernel<3, RtFFT<12>><<<grid, blk, lsm(a.L, a.plc.m, 2), s>>>(a);
+    else if (a.mode == 0) vz_xspec_conv_kernel<3, RtFFT<16>><<<grid, blk, lsm(a.L, a.plc.m, 2), s>>>(a);
+    else if (r12) vz_xspec_conv_kernel<1, RtFFT<12>><<<grid, blk, lsm(a.L, a.plc.m, 1), s>>>(a);
+    else vz_xspec_conv_kernel<1, RtFFT<16>><<<grid, blk, lsm(a.L, a.plc.m, 1), s>>>(a);
 }
 void launch_vz_convtab(const VtabArgs& a, cudaStream_t s) {
     vz_convtab_kernel<<<(a.nzh + a.L - 1) / a.L, dim3(max(a.pl.tx, a.plc.tx), a.L), lsm(a.L, max(a.pl.m, a.plc.m), 1), s>>>(a);
 }
 void launch_vz_passB(const VzArgsB& a, cudaStream_t s) {
     const dim3 blk(a.pl.tx, a.L);
-    if (plan_max_radix(a.pl) <= 12) vz_passB_kernel<12><<<zgrid(a.nxx, a.L), blk, lsm(a.L, a.pl.m, 2), s>>>(a);
-    else vz_passB_kernel<16><<<zgrid(a.nxx, a.L), blk, lsm(a.L, a.pl.m, 2), s>>>(a);
+    const size_t sm = lsm(a.L, a.pl.m, 2);
+#define L_(FPT) vz_passB_kernel<FPT><<<zgrid(a.nxx, a.L), blk, sm, s>>>(a)
+    QP_DISPATCH(ZPlans, a.pl, NoExtraPlan{}, plan_max_radix(a.pl) <= 12, L_);
+#undef L_
 }
 void launch_vz_passC(const VzArgsC& a, cudaStream_t s) {
     const dim3 blk(a.pl.tx, a.L);
-    if (plan_max_radix(a.pl) <= 12) vz_passC_kernel<12><<<zgrid(a.nxx, a.L), blk, lsm(a.L, a.pl.m, 1), s>>>(a);
-    else vz_passC_kernel<16><<<zgrid(a.nxx, a.L), blk, lsm(a.L, a.pl.m, 1), s>>>(a);
+    const size_t sm = lsm(a.L, a.pl.m, 1);
+#define L_(FPT) vz_passC_kernel<FPT><<<zgrid(a.nxx, a.L), blk, sm, s>>>(a)
+    QP_DISPATCH(ZPlans, a.pl, NoExtraPlan{}, plan_max_radix(a.pl) <= 12, L_);
+#undef L_
 }
 void launch_vz_zinv(const VzArgsI& a, cudaStream_t s) {
     const dim3 blk(a.pl.tx, a.L);
-    if (plan_max_radix(a.pl) <= 12) vz_zinv_kernel<12><<<zgrid(a.nxx, a.L), blk, lsm(a.L, a.pl.m, 1), s>>>(a);
-    else vz_zinv_kernel<16><<<zgrid(a.nxx, a.L), blk, lsm(a.L, a.pl.m, 1), s>>>(a);
+    const size_t sm = lsm(a.L, a.pl.m, 1);
+#define L_(FPT) vz_zinv_kernel<FPT><<<zgrid(a.nxx, a.L), blk, sm, s>>>(a)
+    QP_DISPATCH(ZPlans, a.pl, NoExtraPlan{}, plan_max_radix(a.pl) <= 12, L_);
+#undef L_
+}
+
+template <class FP> static int vz_set_limits_one() {
+    const int lim = 200 * 1024;
+    int bad = 0;
+    bad |= cudaFuncSetAttribute(vz_passA_kernel<FP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_passB_kernel<FP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_passC_kernel<FP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_zinv_kernel<FP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
+    return bad;
 }
 
 int vz_set_smem_limits() {
-    int bad = 0;
-    bad |= cudaFuncSetAttribute(vz_passA_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_passA_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_xspec_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_xspec_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<3, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<3, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<1, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<1, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_convtab_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_passB_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_passB_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_passC_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_passC_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_zinv_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_zinv_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess;
+    const int lim = 200 * 1024;
+    int bad = vz_set_limits_one<RtFFT<12>>() | vz_set_limits_one<RtFFT<16>>();
+    for_each_plan(ZPlans{}, [&](auto fp) { bad |= vz_set_limits_one<decltype(fp)>(); });
+    bad |= cudaFuncSetAttribute(vz_xspec_kernel<RtFFT<12>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_xspec_kernel<RtFFT<16>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<3, RtFFT<12>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<3, RtFFT<16>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<1, RtFFT<12>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<1, RtFFT<16>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_convtab_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
     return bad ? -1 : 0;
 }
 
