@@ -10,6 +10,10 @@
 // negative-frequency shift phases.
 #include "host_setup.h"
 
+#include <initializer_list>
+
+#include "xplans_list.h"
+
 #include <algorithm>
 #include <cmath>
 #include <complex>
@@ -276,6 +280,22 @@ int build_plan_host(int n, HostPlan& hp) {
 // one zero-padded forward and one inverse length-m FFT (every lag i-j in
 // (-n, n) lands on a distinct slot of the length-m wrap), so a window length
 // with a large prime factor costs two smooth FFTs instead of Bluestein's four.
+// Lengths whose convolution passes are compiled with the plan built in
+// (xplans_list.h): their passes run about a fifth faster than the run-time plan
+// (measured on the z passes), which the planner counts as a lower cost.
+#define QP_XPLAN_PRODUCT(...) qp_product({__VA_ARGS__}),
+static int qp_product(std::initializer_list<int> r) {
+    int m = 1;
+    for (int x : r) m *= x;
+    return m;
+}
+static bool compiled_conv_length(int m) {
+    static const int lens[] = {QP_XPLANS_ALL(QP_XPLAN_PRODUCT)};
+    for (int x : lens)
+        if (x == m) return true;
+    return false;
+}
+
 int build_conv_plan_host(int n, HostPlan& hp) {
     hp = HostPlan();
     hp.n = n;
@@ -288,7 +308,8 @@ int build_conv_plan_host(int n, HostPlan& hp) {
             if (!smooth7(m)) continue;
             std::vector<int> r;
             if (!factor_direct(m, r)) continue;
-            const double cost = (double)m * r.size() * radix_weight(r);
+            double cost = (double)m * r.size() * radix_weight(r);
+            if (compiled_conv_length(m)) cost *= 0.8;
             if (cost < best) {
                 best = cost;
                 hp.m = m;

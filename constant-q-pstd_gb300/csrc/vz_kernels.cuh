@@ -1,0 +1,349 @@
+// vz_kernels.cuh -- fused passes of the constant-Q (vaps / qrtm) step.
+//
+// Reference step (sgpstd-qmodeling/acsglw.cu:511-645, sgpstd-qrtm/acsglw.cu:511-657):
+//   div   = dx- vx + dz- vz (+ CPML)
+//   Y2,Y3,Y4 = F^-1[(k^2)^(1/32), k^2, (k^2)^(33/32) . F div]       (3 inverse 2-D FFTs)
+//   total = (1-32g) div + 32g vwd Y2 - dt^2 vp^2 lam/12 ((1-64g) Y3 + 64g vwd Y4)
+//   D     = F^-1[(k^2)^0.505 F total]
+//   p    += rho vp^2 dt lam (total -/+ dt tau D/2) -/+ dt tau aux     (vaps / qrtm)
+//   Px,Pz = staggered gradients of p (+ CPML), v update
+//   aux   = F^-1[(k^2)^0.505 F p]  (vaps)  or the stabilised filter S(k,t) (qrtm)
+// Here: z pass A (div, z-FFT), x-spectral pass (3 symbols), z pass B (total,
+// z-FFT), x-spectral pass (k^0.505), z pass C (D, p update, z-FFT of p, Pz and
+// vz update), x pass (Px, vx update, next Dx; shared with the acoustic step),
+// x-spectral pass (aux symbol).  The aux spectrum is turned back into a real
+// field at the start of the next step's z pass A.
+//
+// Half spectra: S[ix*nzh + kz], kz in [0, nzz/2].  Two real z-lines a, b are
+// transformed as one complex line z = a + ib; A(k) = (Z(k) + conj Z(n-k))/2,
+// B(k) = (Z(k) - conj Z(n-k))/(2i), and back Z(k) = A(k) + iB(k).
+#pragma once
+#include "fft_reg.cuh"
+#include "pass_common.cuh"
+
+namespace qp {
+
+#define ZPASS_SETUP                                                  \
+    extern __shared__ float2 smem[];                                 \
+    __shared__ FFTPass s_pass[QP_MAXST];                             \
+    const FFTCtx fc = make_ctx(a.pl, s_pass);                        \
+    const int L = a.L, ld = a.pl.m, nzz = a.nzz, nxx = a.nxx;        \
+    float2* line = smem + threadIdx.y * ld;                          \
+    const int xa = blockIdx.x * 2 * L + 2 * threadIdx.y;             \
+    const bool has0 = xa < nxx, has1 = xa + 1 < nxx;                 \
+    const size_t r0 = (size_t)xa * nzz, r1 = r0 + nzz;               \
+    (void)r1;
+
+// ---- z pass A ---------------------------------------------------------------
+template <class FP>
+__global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passA_kernel(VzArgsA a) {
+    extern __shared__ float2 smem[];
+    __shared__ FFTPass s_pass[QP_MAXST];
+    __shared__ FFTPass s_pass_c[QP_MAXST];
+    const FFTCtx fc = make_ctx(a.pl, s_pass);
+    const FFTCtx fcc = make_ctx(a.plc, s_pass_c);
+    const int L = a.L, ld = max(a.pl.m, a.plc.m), nzz = a.nzz, nxx = a.nxx;
+    float2* line = smem + threadIdx.y * ld;
+    const int xa = blockIdx.x * 2 * L + 2 * threadIdx.y;
+    const bool has0 = xa < nxx, has1 = xa + 1 < nxx;
+    const size_t r0 = (size_t)xa * nzz, r1 = r0 + nzz;
+    const int nzh = a.nzh;
+    if (a.aux_spec) {
+        zrepack(a.aux_spec, line, nzz, nzh, has0, has1, xa);
+        __syncthreads();
+        dft_n<+1, FP>(smem, ld, fc, L);
+        for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+            const float2 v = line[k];
+            if (has0) a.aux[r0 + k] = v.x;
+            if (has1) a.aux[r1 + k] = v.y;
+        }
+        __syncthreads();
+    }
+    zload_pair(a.vz, line, nzz, has0, has1, r0, r1);
+    __syncthreads();
+    roundtrip_conv<FP>(smem, ld, fcc, L, a.HzM);
+    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+        const float2 d = line[k];
+        const float ib = a.i_bz[k], ia = a.i_az[k];
+        float2 dv = make_float2(0.f, 0.f);
+        if (has0) {
+            const float ps = ib * a.psi_vz[r0 + k] + ia * d.x;
+            a.psi_vz[r0 + k] = ps;
+            dv.x = a.Dx[r0 + k] + (d.x + ps);
+            a.div[r0 + k] = dv.x;
+        }
+        if (has1) {
+            const float ps = ib * a.psi_vz[r1 + k] + ia * d.y;
+            a.psi_vz[r1 + k] = ps;
+            dv.y = a.Dx[r1 + k] + (d.y + ps);
+            a.div[r1 + k] = dv.y;
+        }
+        line[k] = dv;
+    }
+    __syncthreads();
+    dft_n<-1, FP>(smem, ld, fc, L);
+    zunpack(line, a.G, nzz, nzh, has0, has1, xa);
+}
+
+// ---- x-spectral pass ----------------------------------------------------------
+// L kz columns per CTA (L a power of two); line c = column kz0 + c.
+__device__ __forceinline__ float spec_symbol(const VxsArgs& a, int j, float k2) {
+    if (a.mode == 0) {
+        if (j == 1) return k2;
+        const float k32 = exp2f(log2f(k2) * (1.f / 32.f));
+        return (j == 0) ? k32 : k2 * k32;
+    }
+    const float ka = exp2f(0.505f * log2f(k2));
+    if (a.mode == 1) return ka;
+    const float num = 2.f * a.eta6 * ka * (1.f + a.tao * a.dt * ka);
+    const float den = expf(-a.tao * a.tt * ka) + a.eta6 * expf(a.tao * a.dt * ka);
+    return ka - num / den;
+}
+
+// FP: transform policy of the exact plan (Bluestein plans included).
+template <class FP>
+__global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_PASS_REGS : QP_EXACT_REGS) vz_xspec_kernel(VxsArgs a) {
+    extern __shared__ float2 smem[];
+    __shared__ FFTPass s_pass[QP_MAXST];
+    const FFTCtx fc = make_ctx(a.pl, s_pass);
+    const int L = a.L, ld = a.pl.m, nxx = a.nxx, nzh = a.nzh;
+    const int lg = 31 - __clz(L);
+    const int kz0 = blockIdx.x * L;
+    const int t0 = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+    const int tot = L * nxx;
+    const int nout = (a.mode == 0) ? 3 : 1;
+    float2* X = smem + (size_t)L * ld;  // kept forward spectrum (three-output mode)
+    float2* line = smem + threadIdx.y * ld;
+    for (int g = t0; g < tot; g += nthr) {
+        const int c = g & (L - 1), ix = g >> lg;
+        const int kz = kz0 + c;
+        smem[c * ld + ix] = (kz < nzh) ? a.in[(size_t)ix * nzh + kz] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    dft_n<-1, FP>(smem, ld, fc, L);
+    if (nout == 3) {
+        for (int ix = threadIdx.x; ix < nxx; ix += blockDim.x) X[threadIdx.y * ld + ix] = line[ix];
+        __syncthreads();
+    }
+    // Outputs written out in sequence (a loop here costs register spills); the
+    // indices are formed again inside each, so that none is held across the
+    // transforms (this keeps the kernel within its register cap).
+    auto output = [&](int j) __attribute__((always_inline)) {
+        const int L = a.L, ld = a.pl.m, nzh = a.nzh, nxx = a.nxx;
+        float2* out = (j == 0) ? a.out0 : (j == 1) ? a.out1 : a.out2;
+        {
+            const int kz = blockIdx.x * L + threadIdx.y;
+            const float kzsq = a.kz2[(kz < nzh) ? kz : 0];
+            float2* ln = smem + threadIdx.y * ld;
+            const float2* src = (a.mode == 0) ? smem + (size_t)(L + threadIdx.y) * ld : ln;
+            for (int ix = threadIdx.x; ix < nxx; ix += blockDim.x)
+                ln[ix] = cscale(src[ix], spec_symbol(a, j, a.kx2[ix] + kzsq) * a.norm);
+        }
+        __syncthreads();
+        dft_n<+1, FP>(smem, ld, fc, L);
+        const int lgl = 31 - __clz(L), kzb = blockIdx.x * L, tl = L * nxx;
+        for (int g = threadIdx.y * blockDim.x + threadIdx.x; g < tl; g += blockDim.x * blockDim.y) {
+            const int c = g & (L - 1), ix = g >> lgl;
+            if (kzb + c < nzh) out[(size_t)ix * nzh + kzb + c] = smem[c * ld + ix];
+        }
+        __syncthreads();
+    };
+    output(0);
+    if (nout == 3) {
+        output(1);
+        output(2);
+    }
+}
+
+// ---- x-spectral pass, stationary symbols as per-kz convolutions ---------------
+// A stationary symbol s(kx, kz) acts on one kz column as a circular
+// convolution along x, so a zero-padded FFT on the smooth convolution length
+// replaces the exact (Bluestein) DFTs: one forward transform, then per output a
+// multiply by the column's table and one inverse transform.
+// NOUT = 3 (mode 0) or 1 (mode 1): each instance carries only the transforms it runs.
+// FP: transform policy of the convolution plan.
+template <int NOUT, class FP>
+__global__ void __maxnreg__(NOUT == 3 ? QP_WIDE_REGS : FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS)
+    vz_xspec_conv_kernel(VxsArgs a) {
+    extern __shared__ float2 smem[];
+    __shared__ FFTPass s_pass[QP_MAXST];
+    const FFTCtx fc = make_ctx(a.plc, s_pass);
+    const int L = a.L, m = a.plc.m, ld = m, nxx = a.nxx, nzh = a.nzh;
+    const int lg = 31 - __clz(L);
+    const int kz0 = blockIdx.x * L;
+    const int t0 = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+    const int tot = L * nxx;
+    constexpr int nout = NOUT;
+    float2* X = smem + (size_t)L * ld;  // kept forward spectrum (three-output mode)
+    float2* line = smem + threadIdx.y * ld;
+    for (int g = t0; g < tot; g += nthr) {
+        const int c = g & (L - 1), ix = g >> lg;
+        const int kz = kz0 + c;
+        smem[c * ld + ix] = (kz < nzh) ? a.in[(size_t)ix * nzh + kz] : make_float2(0.f, 0.f);
+    }
+    for (int k = nxx + threadIdx.x; k < m; k += blockDim.x) line[k] = make_float2(0.f, 0.f);
+    __syncthreads();
+    fft_m<-1, FP>(smem, ld, fc, L);
+    const int kz = min(kz0 + (int)threadIdx.y, nzh - 1);
+    if (nout == 3) {
+        for (int k = threadIdx.x; k < m; k += blockDim.x) X[threadIdx.y * ld + k] = line[k];
+        __syncthreads();
+    }
+    // the multipliers are even in k: rows hold entries 0..m/2
+    const int mh = m / 2 + 1;
+    auto output = [&](const float* __restrict__ tab, float2* out) {
+        const float2* src = (nout == 3) ? X + threadIdx.y * ld : line;
+        const float* tk = tab + (size_t)kz * mh;
+        for (int k = threadIdx.x; k < m; k += blockDim.x) line[k] = cscale(src[k], __ldg(&tk[min(k, m - k)]));
+        __syncthreads();
+        fft_m<+1, FP>(smem, ld, fc, L);
+        for (int g = t0; g < tot; g += nthr) {
+            const int c = g & (L - 1), ix = g >> lg;
+            if (kz0 + c < nzh) out[(size_t)ix * nzh + kz0 + c] = smem[c * ld + ix];
+        }
+        __syncthreads();
+    };
+    output(a.tab0, a.out0);
+    if (nout == 3) {
+        output(a.tab1, a.out1);
+        output(a.tab2, a.out2);
+    }
+}
+
+// ---- z pass B -----------------------------------------------------------------
+template <class FP>
+__global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passB_kernel(VzArgsB a) {
+    ZPASS_SETUP
+    const int nzh = a.nzh;
+    float2* acc = smem + (size_t)(L + threadIdx.y) * ld;  // running total of this line pair
+    // three terms, written out in sequence (a loop here costs register spills)
+    auto term = [&](const float2* spec, const float* cf, float sg, bool first) {
+        zrepack(spec, line, nzz, nzh, has0, has1, xa);
+        __syncthreads();
+        dft_n<+1, FP>(smem, ld, fc, L);
+        for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+            const float2 y = line[k];
+            float2 t = first ? make_float2(0.f, 0.f) : acc[k];
+            if (has0) t.x += sg * cf[r0 + k] * y.x;
+            if (has1) t.y += sg * cf[r1 + k] * y.y;
+            acc[k] = t;
+        }
+        __syncthreads();
+    };
+    term(a.Y2, a.y2, 1.f, true);
+    term(a.Y3, a.y3c, -1.f, false);
+    term(a.Y4, a.y4c, -1.f, false);
+    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+        const float2 t = acc[k];
+        float2 v = make_float2(0.f, 0.f);
+        if (has0) {
+            v.x = a.y1[r0 + k] * a.div[r0 + k] + t.x;
+            a.total[r0 + k] = v.x;
+        }
+        if (has1) {
+            v.y = a.y1[r1 + k] * a.div[r1 + k] + t.y;
+            a.total[r1 + k] = v.y;
+        }
+        line[k] = v;
+    }
+    __syncthreads();
+    dft_n<-1, FP>(smem, ld, fc, L);
+    zunpack(line, a.T, nzz, nzh, has0, has1, xa);
+}
+
+// ---- z pass C -----------------------------------------------------------------
+template <class FP>
+__global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passC_kernel(VzArgsC a) {
+    ZPASS_SETUP
+    const int nzh = a.nzh;
+    zrepack(a.Dspec, line, nzz, nzh, has0, has1, xa);
+    __syncthreads();
+    dft_n<+1, FP>(smem, ld, fc, L);
+    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+        const float2 D = line[k];
+        float2 pn = make_float2(0.f, 0.f);
+        if (has0) {
+            const size_t i = r0 + k;
+            pn.x = a.p[i] + a.e1[i] * (a.total[i] + a.sgn * a.e2[i] * D.x) + a.sgn * a.e3[i] * a.aux[i];
+            if (xa == a.xs && k == a.zs) pn.x += a.src;
+        }
+        if (has1) {
+            const size_t i = r1 + k;
+            pn.y = a.p[i] + a.e1[i] * (a.total[i] + a.sgn * a.e2[i] * D.y) + a.sgn * a.e3[i] * a.aux[i];
+            if (xa + 1 == a.xs && k == a.zs) pn.y += a.src;
+        }
+        line[k] = pn;
+    }
+    __syncthreads();
+    const int ix0 = blockIdx.x * 2 * L;
+    if (a.rec_off) {
+        float* sf = reinterpret_cast<float*>(smem);
+        const int t0 = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+        const int q0 = a.rec_off[blockIdx.x], q1 = a.rec_off[blockIdx.x + 1];
+        for (int q = q0 + t0; q < q1; q += nthr) {
+            const RecEntry e = a.rec[q];
+            const int rel = e.gx - ix0;
+            const int si = 2 * ((rel >> 1) * ld + e.gz) + (rel & 1);
+            if (a.gather_row) a.gather_row[e.ir] = sf[si];
+            if (a.obs_row && e.inject) sf[si] = a.obs_row[e.ir];
+        }
+        __syncthreads();
+    }
+    const int pml = a.pml, nz = nzz - 2 * pml;
+    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+        const float2 pn = line[k];
+        for (int h = 0; h < 2; h++) {
+            const int ix = xa + h;
+            if (ix >= nxx) break;
+            const float v = h ? pn.y : pn.x;
+            const size_t i = (size_t)ix * nzz + k;
+            a.p[i] = v;
+            if (ix >= pml && ix < nxx - pml && k >= pml && k < nzz - pml) {
+                const size_t j = (size_t)(ix - pml) * nz + (k - pml);
+                if (a.ssg) kahan_add(a.ssg, a.ssg_c, j, v * v);
+                if (a.img) kahan_add(a.img, a.img_c, j, a.ps[i] * v);
+            }
+        }
+    }
+    __syncthreads();
+    // forward z transform of the new p: half spectrum for the aux operator and
+    // the staggered z derivative from the same transform
+    dft_n<-1, FP>(smem, ld, fc, L);
+    zunpack(line, a.P, nzz, nzh, has0, has1, xa);
+    __syncthreads();
+    for (int k = threadIdx.x; k < nzz; k += blockDim.x) line[k] = cmul(line[k], __ldg(&a.HzP[k]));
+    __syncthreads();
+    dft_n<+1, FP>(smem, ld, fc, L);
+    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+        const float2 d = line[k];
+        const float hb = a.h_bz[k], ha = a.h_az[k];
+        if (has0) {
+            const size_t i = r0 + k;
+            const float ps = hb * a.psi_pz[i] + ha * d.x;
+            a.psi_pz[i] = ps;
+            a.vz[i] = a.vz[i] + a.dt * a.bbz[i] * (d.x + ps);
+        }
+        if (has1) {
+            const size_t i = r1 + k;
+            const float ps = hb * a.psi_pz[i] + ha * d.y;
+            a.psi_pz[i] = ps;
+            a.vz[i] = a.vz[i] + a.dt * a.bbz[i] * (d.y + ps);
+        }
+    }
+}
+
+// ---- z inverse only -------------------------------------------------------------
+template <class FP>
+__global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz_zinv_kernel(VzArgsI a) {
+    ZPASS_SETUP
+    zrepack(a.spec, line, nzz, a.nzh, has0, has1, xa);
+    __syncthreads();
+    dft_n<+1, FP>(smem, ld, fc, L);
+    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+        const float2 v = line[k];
+        if (has0) a.out[r0 + k] = v.x;
+        if (has1) a.out[r1 + k] = v.y;
+    }
+}
+
+}  // namespace qp
