@@ -12,8 +12,10 @@ timed region.  `cpu_baseline` times the FP64 C oracle (a CPU restatement of the
 reference's update equations) on the machine's host cores.
 
 --impl reference times the reference arm: the reference has no CPU stepping
-path and its cuFFT build cannot be compiled on the GPU machine (its sources are not
-shipped), so the arm runs the oracle port of its equations on all host cores.
+path (every step runs on a GPU through cuFFT), so the arm runs the oracle, the
+FP64 port of its equations, on all host cores, one step of shot 0 per bench
+step.  The reference's own cuFFT programs, built and run on the GB300 for the
+first two configurations, are timed separately (tests/golden/make_reference_gpu.py).
 """
 from __future__ import annotations
 
@@ -164,24 +166,6 @@ def allreduce_max(ws, v: float) -> float:
     return float(t.item())
 
 
-def crop(d: dict, max_cols: int) -> dict:
-    """The same shot on at most max_cols columns of its window (source kept inside)."""
-    if d["nxx"] <= max_cols:
-        return d
-    dd = dict(d)
-    nxx, nzz = d["nxx"], d["nzz"]
-    x0 = max(0, min(d["xsg"] - max_cols // 2, nxx - max_cols))
-    for k in ("vp", "rho", "bbx", "bbz", "gam", "lam", "vwd", "tao"):
-        if d.get(k) is not None:
-            dd[k] = np.asarray(d[k]).reshape(nxx, nzz)[x0:x0 + max_cols].ravel()
-    keep = (np.asarray(d["gxg"]) >= x0) & (np.asarray(d["gxg"]) < x0 + max_cols)
-    dd["gxg"] = (np.asarray(d["gxg"])[keep] - x0).astype(np.int32)
-    dd["gzg"] = np.asarray(d["gzg"])[keep]
-    dd["xsg"] = d["xsg"] - x0
-    dd["nxx"] = max_cols
-    return dd
-
-
 def oracle_rate(d: dict, kname: str, nsteps: int):
     """FP64 oracle time steps on the host cores: (Gpts/s, seconds)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -242,7 +226,7 @@ def run_reference(args, ws, rank):
     if rank != 0:
         return
     shots, kname, seed, desc, _ = workload(args.workload)
-    d = crop(shots[0], 600)
+    d = shots[0]
     per = []
     for i in range(args.warmup + args.steps):
         _, el = oracle_rate(d, kname, 1)
@@ -256,8 +240,8 @@ def run_reference(args, ws, rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": f"synthetic (seed {seed})",
         "config": desc,
         "cpu_baseline": {"value": val, "unit": "Gpts/s", "cores": os.cpu_count(), "kind": "port",
-                         "sample": f"one FP64 oracle time step per bench step on a {d['nxx']}x{d['nzz']} "
-                                   f"window of shot 0 of the workload"},
+                         "sample": f"one FP64 oracle time step of shot 0 of the workload ({d['nxx']}x{d['nzz']}, "
+                                   f"the whole window) per bench step"},
         "e2e": {"value": val, "unit": "Gpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
@@ -370,7 +354,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="qrtm4")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--e2e-shots", type=int, default=16)
+    ap.add_argument("--e2e-shots", type=int, default=0, help="RTM workloads: shots in the e2e call (0: all)")
+    ap.add_argument("--plain-shots", type=int, default=2,
+                    help="RTM workloads: whole plain-form shots timed for the per-shot shots/hour")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--shots", type=int, default=0,
@@ -413,8 +399,6 @@ def main():
         t += 1
     B.sync()
     barrier(ws)
-    for i in range(len(shots)):
-        qpstd.lib().qpstd_shot_set_profiling(B.shot(i), 1)
     launches0 = sum(int(qpstd.lib().qpstd_shot_launch_count(B.shot(i))) for i in range(len(shots)))
     step_ms = []
     # the timed steps are the profiler's range (ncu --profile-from-start off
@@ -462,18 +446,6 @@ def main():
             t += 1
     torch.cuda.profiler.stop()
     launches = sum(int(qpstd.lib().qpstd_shot_launch_count(B.shot(i))) for i in range(len(shots))) - launches0
-    kern = {}
-    for i in range(len(shots)):
-        n = len(qpstd.KIND_NAMES)
-        ms = (qpstd.C.c_double * n)()
-        cnt = (qpstd.C.c_longlong * n)()
-        qpstd.lib().qpstd_shot_profile_read(B.shot(i), n, ms, cnt)
-        for k in range(n):
-            if cnt[k]:
-                a = kern.setdefault(qpstd.KIND_NAMES[k], [0.0, 0])
-                a[0] += ms[k]
-                a[1] += cnt[k]
-        qpstd.lib().qpstd_shot_set_profiling(B.shot(i), 0)
     B.pipeline_end()
     B.sync()
     total_ms = allreduce_max(ws, sum(step_ms))
@@ -487,10 +459,14 @@ def main():
         pass
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    # per-kernel: summed launch time over all shots and steps (kernels of different
-    # shots overlap, so these sums exceed the wall time of a step)
-    kernels = {k: {"launches": v[1], "ms_sum": v[0], "ms_avg": v[0] / v[1]} for k, v in kern.items()}
-    dom = max(kernels, key=lambda k: kernels[k]["ms_sum"])
+    # the dominant kernel: the largest share of the serialised launch list that
+    # ncu recorded for this workload (profiles/launches_<workload>.json)
+    dom = None
+    try:
+        lj = json.load(open(os.path.join(ROOT, "profiles", f"launches_{args.workload}.json")))
+        dom = max(lj["kernels"], key=lambda k: k["share"])["name"]
+    except (OSError, KeyError, ValueError):
+        pass
     alg = ALG_BYTES_STEP[kname] * pts
     achieved = alg / (ms_per_step / 1000.0) / 1e9
     traffic = None
@@ -523,7 +499,6 @@ def main():
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": peak_src, "alg_bytes_per_point": ALG_BYTES_STEP[kname],
                      "traffic": traffic, "dominant": dom},
-        "kernels": kernels,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
@@ -552,10 +527,11 @@ def main():
         out["plain_per_shot"] = {"ms_per_step_shot0": pms, "gpts_per_s": d0["nxx"] * d0["nzz"] / pms / 1e6,
                                  "note": "cuFFT 2-D C2C + elementwise kernels in the reference's order, "
                                          "one shot at a time (shot 0 of the workload)"}
+    work_of = lambda d: d["nxx"] * d["nzz"] * 2 * d["nt"]  # Gpts counted as 2*nt per RTM shot
     # ---- end to end through the C ABI with host buffers ----
     if not args.no_e2e:
         if kname in ("artm", "qrtm"):
-            ne = min(args.e2e_shots, len(shots))
+            ne = len(shots) if args.e2e_shots <= 0 else min(args.e2e_shots, len(shots))
             sub = shots[:ne]
             obs = [obs_maker(d, i) for i, d in enumerate(sub)]
             torch.cuda.synchronize()
@@ -564,13 +540,40 @@ def main():
             imgs, ssgs = qpstd.rtm_batch(sub, obs)
             torch.cuda.synchronize()
             wall = allreduce_max(ws, time.perf_counter() - t0)
-            work = sum(d["nxx"] * d["nzz"] * 2 * d["nt"] for d in sub)
+            work = sum(work_of(d) for d in sub)
             h2d = sum(4 * (12 * d["nxx"] * d["nzz"] + d["nt"]) + 4 * o.size for d, o in zip(sub, obs))
             d2h = sum(4 * 2 * im.size for im in imgs)
             out["e2e"] = {"value": ws * work / wall / 1e9, "unit": "Gpts/s", "wall_s": wall, "shots": ne,
                           "shots_per_hour": ws * 3600.0 * ne / wall, "h2d_bytes_per_step": h2d,
                           "d2h_bytes_per_step": d2h,
-                          "step": f"one call of qpstd_rtm_batch on {ne} shots (Gpts counted as 2*nt per shot)"}
+                          "step": f"one call of qpstd_rtm_batch on {ne} shots (whole Q-RTM: revolve recompute, "
+                                  f"receiver side, imaging; Gpts counted as 2*nt per shot)"}
+            # whole plain-form shots, one at a time, through the same C ABI: the
+            # per-shot shots/hour of the workload, from the measured seconds per
+            # grid-point step (every shot has the same nt and snapshot count, so an
+            # RTM shot's work is proportional to its points)
+            if not args.no_plain and args.plain_shots > 0:
+                pw, pt = 0.0, 0.0
+                for i in range(min(args.plain_shots, len(shots))):
+                    d = shots[i]
+                    o = obs_maker(d, i)
+                    t1 = time.perf_counter()
+                    qpstd.rtm_shot(d, o, method=qpstd.PLAIN)
+                    pt += time.perf_counter() - t1
+                    pw += work_of(d)
+                per_work = pt / pw
+                total = per_work * sum(work_of(d) for d in shots)
+                plain_sph = 3600.0 * len(shots) / total
+                out["plain_per_shot"].update({
+                    "rtm_shots_timed": min(args.plain_shots, len(shots)), "rtm_wall_s": pt,
+                    "rtm_shots_per_hour": plain_sph,
+                    "rtm_note": f"whole plain-form Q-RTM shots 0..{min(args.plain_shots, len(shots)) - 1} through "
+                                f"qpstd_rtm_shot with host buffers, one at a time; shots/hour of the whole "
+                                f"{len(shots)}-shot workload extrapolated by points"})
+                if ne == len(shots):
+                    out["batched_vs_per_shot"] = {"shots_per_hour": out["e2e"]["shots_per_hour"],
+                                                  "per_shot_shots_per_hour": plain_sph,
+                                                  "ratio": out["e2e"]["shots_per_hour"] / plain_sph}
         else:
             t0 = time.perf_counter()
             g = qpstd.model_shot(shots[0])
