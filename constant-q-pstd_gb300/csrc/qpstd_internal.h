@@ -180,11 +180,34 @@ struct VxsArgs {
 // plc.m, then out[kz*mh + k] = Re FFT_m(h)[k] / m for k = 0..m/2, mh = m/2+1
 // (h is real and even, so the multipliers are real and even in k).
 struct VtabArgs {
-    int nxx, nzz, nzh, L, sym;  // sym: 0 (k^2)^(1/32), 1 k^2, 2 (k^2)^(33/32), 3 (k^2)^0.505
+    int nxx, nzz, nzh, L, sym;  // sym: 0 (k^2)^(1/32), 1 k^2, 2 (k^2)^(33/32), 3 (k^2)^0.505,
+                                //      4 the low-rank factor V (half grid, mirrored in kx)
     FFTPlanDev pl, plc;
     const float *kx2, *kz2;
+    const float* V;             // sym 4: nxh x nzh values of one factor
+    int nxh;
     float norm;
     float* out;
+};
+
+// Low-rank form of the constant-Q pressure term (qpstd_shot_set_lowrank):
+// x-spectral pass: per kz column, Q_b = F_x^-1[Vt_b F_x G] / (nxx nzz) for the
+// row factors b, as per-kz convolutions on the convolution plan (tables built
+// from V by vz_convtab_kernel, sym 4).
+struct LrxArgs {
+    int nxx, nzh, L, row;
+    FFTPlanDev plc;
+    const float2* in;           // G, the z half spectrum of div
+    float2* out;                // row half spectra, factor-major (b * nxx * nzh)
+    const float* tab;           // row x nzh x (plc.m/2+1)
+};
+// z pass: psc(x) = sum_b c_b(x) Re F_z^-1[Q_b](x), c_b(x) = sum_a U[x][a] A[a][b].
+struct LrsArgs {
+    int nxx, nzz, nzh, L, row;
+    FFTPlanDev pl;              // exact length-nzz plan
+    const float2* Q;
+    const float* c;             // row x nxx*nzz
+    float* psc;
 };
 
 // z pass B: Y2, Y3, Y4 from their spectra; total; total -> half spectrum T.
@@ -203,7 +226,7 @@ struct VzArgsB {
 struct VzArgsC {
     int nxx, nzz, nzh, L, pml;
     FFTPlanDev pl;
-    const float2* Dspec;
+    const float2* Dspec;      // null: no loss term (low-rank form: total = W{div}, e1 = rho vp^2 dt)
     const float* total;
     const float* aux;
     float* p;

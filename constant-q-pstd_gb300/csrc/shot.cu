@@ -34,6 +34,8 @@ void launch_vz_passC(const VzArgsC& a, cudaStream_t s);
 void launch_vz_zinv(const VzArgsI& a, cudaStream_t s);
 void launch_vz_xspec_conv(const VxsArgs& a, cudaStream_t s);
 void launch_vz_convtab(const VtabArgs& a, cudaStream_t s);
+void launch_lr_xconv(const LrxArgs& a, cudaStream_t s);
+void launch_lr_zsum(const LrsArgs& a, cudaStream_t s);
 int vz_set_smem_limits();
 }  // namespace qp
 
@@ -719,32 +721,51 @@ static void vz_step(qpstd_shot* s, Wave& w, float src, int t_filter, float eta, 
             launch_vz_xspec(a, st);
         }
     };
-    {
-        VxsArgs a = xs;
-        a.mode = 0; a.L = s->Lxs3;
-        a.in = s->spec[0]; a.out0 = s->spec[1]; a.out1 = s->spec[2]; a.out2 = s->spec[3];
-        xspec(a);
-    }
-    {
-        VzArgsB a{};
-        a.nxx = nxx; a.nzz = nzz; a.nzh = nzh; a.L = s->Lzv; a.pl = s->pz;
-        a.Y2 = s->spec[1]; a.Y3 = s->spec[2]; a.Y4 = s->spec[3];
-        a.div = s->div; a.y1 = s->y1; a.y2 = s->y2; a.y3c = s->y3c; a.y4c = s->y4c;
-        a.total = s->total; a.T = s->spec[0];
+    const bool lowrank = s->lr_row > 0;
+    if (lowrank) {
+        // low-rank form: total <- W{div} = sum_b c_b Re F^-1[Vt_b F div] / N
+        LrxArgs x{};
+        x.nxx = nxx; x.nzh = nzh; x.L = s->Llr; x.row = s->lr_row; x.plc = s->pxc;
+        x.in = s->spec[0]; x.out = s->lr_Q; x.tab = s->lr_tab;
+        {
+            ProfScope ps(s, QPSTD_K_XSPEC);
+            launch_lr_xconv(x, st);
+        }
+        LrsArgs z{};
+        z.nxx = nxx; z.nzz = nzz; z.nzh = nzh; z.L = s->Llrz; z.row = s->lr_row; z.pl = s->pz;
+        z.Q = s->lr_Q; z.c = s->lr_c; z.psc = s->total;
         ProfScope ps(s, QPSTD_K_ZPASS);
-        launch_vz_passB(a, st);
-    }
-    {
-        VxsArgs a = xs;
-        a.mode = 1; a.L = s->Lxs;
-        a.in = s->spec[0]; a.out0 = s->spec[1];
-        xspec(a);
+        launch_lr_zsum(z, st);
+    } else {
+        {
+            VxsArgs a = xs;
+            a.mode = 0; a.L = s->Lxs3;
+            a.in = s->spec[0]; a.out0 = s->spec[1]; a.out1 = s->spec[2]; a.out2 = s->spec[3];
+            xspec(a);
+        }
+        {
+            VzArgsB a{};
+            a.nxx = nxx; a.nzz = nzz; a.nzh = nzh; a.L = s->Lzv; a.pl = s->pz;
+            a.Y2 = s->spec[1]; a.Y3 = s->spec[2]; a.Y4 = s->spec[3];
+            a.div = s->div; a.y1 = s->y1; a.y2 = s->y2; a.y3c = s->y3c; a.y4c = s->y4c;
+            a.total = s->total; a.T = s->spec[0];
+            ProfScope ps(s, QPSTD_K_ZPASS);
+            launch_vz_passB(a, st);
+        }
+        {
+            VxsArgs a = xs;
+            a.mode = 1; a.L = s->Lxs;
+            a.in = s->spec[0]; a.out0 = s->spec[1];
+            xspec(a);
+        }
     }
     {
         VzArgsC a{};
         a.nxx = nxx; a.nzz = nzz; a.nzh = nzh; a.L = s->Lzv; a.pml = s->d.pml; a.pl = s->pz;
-        a.Dspec = s->spec[1]; a.total = s->total; a.aux = w.aux(N); a.p = w.p(N);
-        a.e1 = s->e1; a.e2 = s->e2; a.e3 = s->e3;
+        a.Dspec = lowrank ? nullptr : s->spec[1]; a.total = s->total; a.aux = w.aux(N); a.p = w.p(N);
+        // low-rank form: p += rho vp^2 dt W{div} -/+ dt tau aux (the pressure term of the
+        // reference's dormant addsa_b_kernel, sgpstd-qmodeling/acsglw.cu:1542-1571)
+        a.e1 = lowrank ? s->c1 : s->e1; a.e2 = s->e2; a.e3 = s->e3;
         a.sgn = (s->d.kind == QPSTD_QRTM) ? 1.f : -1.f;
         a.xs = (src != 0.f) ? s->d.xsg : -1; a.zs = s->d.zsg; a.src = src;
         if (gather_row || obs_row) { a.rec_off = s->rec_off_z; a.rec = s->rec_z; }
@@ -1137,6 +1158,61 @@ extern "C" int qpstd_shot_advance(qpstd_shot* s, int t0, int nsteps, float* gath
 }
 
 extern "C" long long qpstd_shot_launch_count(const qpstd_shot* s) { return s ? s->launches : -1; }
+
+// Low-rank form of the pressure term (see qpstd.h).  c_b(x) = sum_a U[x][a] A[a][b]
+// is formed once in FP64 (the reference accumulates these sums in double,
+// sumlw_kernel / sumlw2_kernel, sgpstd-qmodeling/acsglw.cu:1444-1497); each V_b,
+// mirrored to the full kx range (consist_Vt, sglowrank.c:103-145), becomes a
+// per-kz convolution table on the x convolution plan.
+extern "C" int qpstd_shot_set_lowrank(qpstd_shot* s, int row, int col, const float* U, const float* V,
+                                      const double* A) {
+    if (!s) return fail(QPSTD_EINVAL, "null shot");
+    if (!s->visco || s->d.method != QPSTD_FUSED)
+        return fail(QPSTD_EINVAL, "the low-rank form applies to fused constant-Q shots (VAPS, QRTM)");
+    if (row < 1 || col < 1 || row > 16 || col > 16 || !U || !V || !A)
+        return fail(QPSTD_EINVAL, "low-rank factors: 1 <= row, col <= 16 and U, V, A non-null");
+    if (s->lr_row) return fail(QPSTD_EINVAL, "the shot already runs the low-rank form");
+    const int nxx = s->d.nxx, nzz = s->d.nzz, nzh = s->nzh, nxh = nxx / 2 + 1;
+    const size_t N = s->N;
+    const int mc = s->pxc.m, mh = mc / 2 + 1;
+    int rc = QPSTD_OK;
+    float* c = dalloc(s, (size_t)row * N, &rc);
+    float* tab = c ? dalloc(s, (size_t)row * nzh * mh, &rc) : nullptr;
+    float* Q = tab ? dalloc(s, (size_t)row * 2 * nxx * nzh, &rc) : nullptr;
+    float* Vd = Q ? dalloc(s, (size_t)row * nxh * nzh, &rc) : nullptr;
+    if (!Vd) return rc;
+    std::vector<float> hc((size_t)row * N);
+    for (size_t x = 0; x < N; x++)
+        for (int b = 0; b < row; b++) {
+            double acc = 0.0;
+            for (int a = 0; a < col; a++) acc += (double)U[x * col + a] * A[(size_t)a * row + b];
+            hc[(size_t)b * N + x] = (float)acc;
+        }
+    CK(cudaMemcpy(c, hc.data(), sizeof(float) * hc.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(Vd, V, sizeof(float) * (size_t)row * nxh * nzh, cudaMemcpyHostToDevice));
+    VtabArgs a{};
+    a.nxx = nxx; a.nzz = nzz; a.nzh = nzh;
+    a.pl = s->px; a.plc = s->pxc; a.kx2 = s->kxsq; a.kz2 = s->kzsq;
+    a.norm = (float)(1.0 / ((double)nxx * nzz));
+    a.L = choose_L(nzh, std::max(s->px.m, mc), std::max(s->px.tx, s->pxc.tx), 1, false);
+    a.sym = 4;
+    a.nxh = nxh;
+    for (int b = 0; b < row; b++) {
+        a.V = Vd + (size_t)b * nxh * nzh;
+        a.out = tab + (size_t)b * nzh * mh;
+        launch_vz_convtab(a, s->stream);
+    }
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "low-rank tables");
+    s->lr_c = c;
+    s->lr_tab = tab;
+    s->lr_Q = reinterpret_cast<float2*>(Q);
+    s->Llr = choose_L(nzh, mc, s->pxc.tx, 2, true);
+    s->Llrz = choose_L((nxx + 1) / 2, s->pz.m, s->pz.tx, 2, false);
+    s->lr_row = row;
+    return QPSTD_OK;
+}
 
 extern "C" long long qpstd_shot_info(const qpstd_shot* s, int key) {
     if (!s) return -1;

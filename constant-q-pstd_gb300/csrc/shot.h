@@ -94,6 +94,12 @@ struct qpstd_shot {
     const float* xtab[4] = {nullptr, nullptr, nullptr, nullptr};
     // Q-RTM filter: per eta, the last step at which it rounds to k^1.01 (see filter_is_ka)
     std::vector<std::pair<float, int>> ka_steps;
+    // low-rank form of the pressure term (qpstd_shot_set_lowrank): row factors,
+    // point weights c_b (row x N), per-kz convolution tables of the V_b
+    // (row x nzh x (pxc.m/2+1)) and the row half spectra of one step
+    int lr_row = 0, Llr = 1, Llrz = 1;
+    float *lr_c = nullptr, *lr_tab = nullptr;
+    float2* lr_Q = nullptr;
     int* rec_off_z = nullptr;                // receivers keyed by z-pass tile
     qp::RecEntry* rec_z = nullptr;
     // plain (cuFFT) form

@@ -19,7 +19,8 @@ __global__ void __launch_bounds__(768, 1) vz_convtab_kernel(VtabArgs a) {
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
         const double k2 = (double)a.kx2[k] + kzsq;
         double s;
-        if (a.sym == 1) s = k2;
+        if (a.sym == 4) s = a.V[(size_t)((k < a.nxh) ? k : n - k) * a.nzh + (valid ? kz : 0)];
+        else if (a.sym == 1) s = k2;
         else if (a.sym == 0) s = pow(k2, 1.0 / 32.0);
         else if (a.sym == 2) s = pow(k2, 33.0 / 32.0);
         else s = pow(k2, 0.505);
@@ -81,6 +82,24 @@ void launch_vz_xspec_conv(const VxsArgs& a, cudaStream_t s) {
 void launch_vz_convtab(const VtabArgs& a, cudaStream_t s) {
     vz_convtab_kernel<<<(a.nzh + a.L - 1) / a.L, dim3(max(a.pl.tx, a.plc.tx), a.L), lsm(a.L, max(a.pl.m, a.plc.m), 1), s>>>(a);
 }
+void launch_lr_xconv(const LrxArgs& a, cudaStream_t s) {
+    const int grid = (a.nzh + a.L - 1) / a.L;
+    const dim3 blk(a.plc.tx, a.L);
+    const size_t sm = lsm(a.L, a.plc.m, 2);
+    if (plan_max_radix(a.plc) <= 12) lr_xconv_kernel<RtFFT<12>><<<grid, blk, sm, s>>>(a);
+    else lr_xconv_kernel<RtFFT<16>><<<grid, blk, sm, s>>>(a);
+}
+void launch_lr_zsum(const LrsArgs& a, cudaStream_t s) {
+    const dim3 blk(a.pl.tx, a.L);
+    const size_t sm = lsm(a.L, a.pl.m, 2);
+    for (int b0 = 0; b0 < a.row; b0 += 3) {
+        const int nb = min(3, a.row - b0);
+#define L_(FPT) lr_zsum_kernel<FPT><<<zgrid(a.nxx, a.L), blk, sm, s>>>(a, b0, nb)
+        QP_DISPATCH(ZPlans, a.pl, NoExtraPlan{}, plan_max_radix(a.pl) <= 12, L_);
+#undef L_
+    }
+}
+
 void launch_vz_passB(const VzArgsB& a, cudaStream_t s) {
     const dim3 blk(a.pl.tx, a.L);
     const size_t sm = lsm(a.L, a.pl.m, 2);
@@ -110,6 +129,7 @@ template <class FP> static int vz_set_limits_one() {
     bad |= cudaFuncSetAttribute(vz_passB_kernel<FP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_passC_kernel<FP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_zinv_kernel<FP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(lr_zsum_kernel<FP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
     return bad;
 }
 
@@ -124,6 +144,8 @@ int vz_set_smem_limits() {
     bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<1, RtFFT<12>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<1, RtFFT<16>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_convtab_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(lr_xconv_kernel<RtFFT<12>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(lr_xconv_kernel<RtFFT<16>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
     return bad ? -1 : 0;
 }
 

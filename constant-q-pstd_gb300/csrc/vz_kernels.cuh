@@ -256,11 +256,13 @@ template <class FP>
 __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passC_kernel(VzArgsC a) {
     ZPASS_SETUP
     const int nzh = a.nzh;
-    zrepack(a.Dspec, line, nzz, nzh, has0, has1, xa);
-    __syncthreads();
-    dft_n<+1, FP>(smem, ld, fc, L);
+    if (a.Dspec) {
+        zrepack(a.Dspec, line, nzz, nzh, has0, has1, xa);
+        __syncthreads();
+        dft_n<+1, FP>(smem, ld, fc, L);
+    }
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
-        const float2 D = line[k];
+        const float2 D = a.Dspec ? line[k] : make_float2(0.f, 0.f);
         float2 pn = make_float2(0.f, 0.f);
         if (has0) {
             const size_t i = r0 + k;
@@ -343,6 +345,82 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz
         const float2 v = line[k];
         if (has0) a.out[r0 + k] = v.x;
         if (has1) a.out[r1 + k] = v.y;
+    }
+}
+
+// ---- low-rank form ------------------------------------------------------------------
+// x-spectral pass of the low-rank pressure term: one forward transform of the
+// kz column of G, then per factor b a multiply by its per-kz convolution table
+// and an inverse transform (the factor loop keeps one copy of the inverse code).
+template <class FP>
+__global__ void __maxnreg__(QP_WIDE_REGS) lr_xconv_kernel(LrxArgs a) {
+    extern __shared__ float2 smem[];
+    __shared__ FFTPass s_pass[QP_MAXST];
+    const FFTCtx fc = make_ctx(a.plc, s_pass);
+    const int L = a.L, m = a.plc.m, ld = m, nxx = a.nxx, nzh = a.nzh;
+    const int lg = 31 - __clz(L);
+    const int kz0 = blockIdx.x * L;
+    const int t0 = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+    const int tot = L * nxx;
+    float2* X = smem + (size_t)L * ld;  // kept forward spectrum
+    float2* line = smem + threadIdx.y * ld;
+    for (int g = t0; g < tot; g += nthr) {
+        const int c = g & (L - 1), ix = g >> lg;
+        const int kz = kz0 + c;
+        smem[c * ld + ix] = (kz < nzh) ? a.in[(size_t)ix * nzh + kz] : make_float2(0.f, 0.f);
+    }
+    for (int k = nxx + threadIdx.x; k < m; k += blockDim.x) line[k] = make_float2(0.f, 0.f);
+    __syncthreads();
+    fft_m<-1, FP>(smem, ld, fc, L);
+    for (int k = threadIdx.x; k < m; k += blockDim.x) X[threadIdx.y * ld + k] = line[k];
+    const int kz = min(kz0 + (int)threadIdx.y, nzh - 1);
+    const int mh = m / 2 + 1;
+#pragma unroll 1
+    for (int b = 0; b < a.row; b++) {
+        const float* tk = a.tab + ((size_t)b * nzh + kz) * mh;
+        __syncthreads();
+        for (int k = threadIdx.x; k < m; k += blockDim.x)
+            line[k] = cscale(X[threadIdx.y * ld + k], __ldg(&tk[min(k, m - k)]));
+        __syncthreads();
+        fft_m<+1, FP>(smem, ld, fc, L);
+        float2* out = a.out + (size_t)b * nxx * nzh;
+        for (int g = t0; g < tot; g += nthr) {
+            const int c = g & (L - 1), ix = g >> lg;
+            if (kz0 + c < nzh) out[(size_t)ix * nzh + kz0 + c] = smem[c * ld + ix];
+        }
+    }
+}
+
+// z pass of the low-rank pressure term: psc (+)= sum_b c_b(x) q_b(x) over the
+// factors b0 .. b0+nb-1 (nb <= 3), q_b the inverse z transform of half spectrum
+// b; the first launch (b0 = 0) overwrites psc.  The factors are written out in
+// sequence like z pass B's terms: a loop around the transform spills registers.
+template <class FP>
+__global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) lr_zsum_kernel(LrsArgs a, int b0, int nb) {
+    ZPASS_SETUP
+    const int nzh = a.nzh;
+    float2* acc = smem + (size_t)(L + threadIdx.y) * ld;
+    auto term = [&](int b, bool first) {
+        zrepack(a.Q + (size_t)b * nxx * nzh, line, nzz, nzh, has0, has1, xa);
+        __syncthreads();
+        dft_n<+1, FP>(smem, ld, fc, L);
+        const float* cb = a.c + (size_t)b * nxx * nzz;
+        for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+            const float2 v = line[k];
+            float2 t = first ? make_float2(0.f, 0.f) : acc[k];
+            if (has0) t.x = fmaf(__ldg(&cb[r0 + k]), v.x, t.x);
+            if (has1) t.y = fmaf(__ldg(&cb[r1 + k]), v.y, t.y);
+            acc[k] = t;
+        }
+        __syncthreads();
+    };
+    term(b0, true);
+    if (nb > 1) term(b0 + 1, false);
+    if (nb > 2) term(b0 + 2, false);
+    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+        const float2 t = acc[k];
+        if (has0) a.psc[r0 + k] = b0 ? a.psc[r0 + k] + t.x : t.x;
+        if (has1) a.psc[r1 + k] = b0 ? a.psc[r1 + k] + t.y : t.y;
     }
 }
 

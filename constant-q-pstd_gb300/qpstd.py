@@ -77,6 +77,7 @@ EXPORTS = {
     "qpstd_shot_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "qpstd_shot_profile_read": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
     "qpstd_shot_info": (C.c_longlong, [C.c_void_p, C.c_int]),
+    "qpstd_shot_set_lowrank": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _fp, _fp, _dp]),
     "qpstd_batch_create": (C.c_int, [C.POINTER(ShotDesc), C.c_int, C.POINTER(C.c_void_p)]),
     "qpstd_batch_destroy": (C.c_int, [C.c_void_p]),
     "qpstd_batch_size": (C.c_int, [C.c_void_p]),
@@ -277,6 +278,10 @@ class Shot:
         _check(lib().qpstd_shot_profile_read(self.h, n, ms, cnt))
         return {KIND_NAMES[k]: (ms[k], cnt[k]) for k in range(n)}
 
+    def set_lowrank(self, f: dict):
+        """Low-rank form of the pressure term with factors f = lowrank_decompose(...)."""
+        shot_set_lowrank(self.h, f)
+
     def info(self) -> dict:
         """The transforms this shot runs (qpstd_shot_info)."""
         return {k: int(lib().qpstd_shot_info(self.h, i)) for i, k in enumerate(INFO_KEYS)}
@@ -372,6 +377,24 @@ def lowrank_decompose(nxx, nzz, dx, dz, dt, vp, tao, gam, row, col, seed=1):
                                          _f(U), _f(V), A.ctypes.data_as(_dp), jrr.ctypes.data_as(_ip),
                                          irr.ctypes.data_as(_ip)))
     return {"U": U, "V": V, "A": A, "jrr": jrr, "irr": irr, "nxx": nxx, "nzz": nzz, "row": row, "col": col}
+
+
+def shot_set_lowrank(handle, f: dict) -> None:
+    """qpstd_shot_set_lowrank on a shot handle (a Shot's .h or Batch.shot(i))."""
+    U = np.ascontiguousarray(f["U"], dtype=np.float32)
+    V = np.ascontiguousarray(f["V"], dtype=np.float32)
+    A = np.ascontiguousarray(f["A"], dtype=np.float64)
+    _check(lib().qpstd_shot_set_lowrank(handle, A.shape[1], A.shape[0], _f(U), _f(V), A.ctypes.data_as(_dp)))
+
+
+def lowrank_factors(dicts, rank: int, threads: int = 0):
+    """lowrank_decompose for each shot window (host FP64; the decompositions run
+    concurrently, the library releases the interpreter during each)."""
+    from concurrent.futures import ThreadPoolExecutor
+    run = lambda d: lowrank_decompose(d["nxx"], d["nzz"], d["dx"], d["dz"], d["dt"], d["vp"], d["tao"], d["gam"],
+                                      rank, rank)
+    with ThreadPoolExecutor(max_workers=threads or min(16, os.cpu_count() or 1)) as ex:
+        return list(ex.map(run, dicts))
 
 
 def lowrank_check(f, dx, dz, dt, vp, tao, gam, point):

@@ -226,6 +226,18 @@ int qpstd_lowrank_decompose(int nxx, int nzz, float dx, float dz, float dt, cons
 int qpstd_lowrank_check(int nxx, int nzz, float dx, float dz, float dt, int row, int col, const float *U,
                         const double *A, const float *V, const float *vp, const float *tao, const float *gam,
                         int is, float *We, float *Wa);
+/* Runs a created fused constant-Q shot (VAPS / QRTM) in the low-rank form: the
+ * pressure update becomes p += rho vp^2 dt W{div} -/+ dt tau aux (- modeling,
+ * + Q-compensated RTM, as the power-expansion form), where W{div} = sum_a
+ * U[x][a] sum_b A[a][b] Re F^-1[Vt_b F div] / N is the reference's dormant
+ * low-rank operator (sgpstd-qmodeling/acsglw.cu:1375-1497) applied as its
+ * dormant pressure update applies it (addsa_b_kernel, acsglw.cu:1542-1571; the
+ * reference's call sites, acsglw.cu:367-389, are commented out, so this wiring
+ * is this library's).  U, V, A as qpstd_lowrank_decompose returns them for the
+ * shot's window (row, col <= 16).  The step then runs the low-rank x-spectral
+ * pass and its z sum in place of the power expansion's three passes. */
+int qpstd_shot_set_lowrank(qpstd_shot *s, int row, int col, const float *U, const float *V, const double *A);
+
 /* Device operator out = sum_a U[x][a] sum_b A[a][b] Re F^-1[Vt_b F in](x) / N
  * (the reference's multv_kernel / sumlw_kernel / sumlw2_kernel,
  * sgpstd-qmodeling/acsglw.cu:1375-1497, with Vt_b = consist_Vt of V_b). */

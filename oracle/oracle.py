@@ -35,6 +35,7 @@ class Shot(C.Structure):
         ("nr", C.c_int), ("gxg", _ip), ("gzg", _ip),
         ("etas", C.c_double), ("etar", C.c_double), ("taoc", C.c_double),
         ("snaps", C.c_int),
+        ("lr_row", C.c_int), ("lr_col", C.c_int), ("lr_U", _dp), ("lr_Vt", _dp), ("lr_A", _dp),
     ]
 
 
@@ -154,6 +155,16 @@ class OracleShot:
                 a = np.ascontiguousarray(d[k], dtype=np.float64).ravel()
                 self.arrays[k] = a
                 setattr(s, k, _d(a))
+        lr = d.get("lowrank")
+        if lr is not None:
+            # low-rank factors {"U": N x col, "V": row x nxh*nzh, "A": col x row}
+            from lowrank import mirror
+            U = np.ascontiguousarray(lr["U"], dtype=np.float64)
+            A = np.ascontiguousarray(lr["A"], dtype=np.float64)
+            Vt = np.ascontiguousarray(mirror(lr["V"], d["nxx"], d["nzz"]).reshape(A.shape[1], -1))
+            self.arrays.update(lr_U=U, lr_Vt=Vt, lr_A=A)
+            s.lr_row, s.lr_col = A.shape[1], A.shape[0]
+            s.lr_U, s.lr_Vt, s.lr_A = _d(U), _d(Vt), _d(A)
         gx = np.ascontiguousarray(d["gxg"], dtype=np.int32)
         gz = np.ascontiguousarray(d["gzg"], dtype=np.int32)
         self.arrays["gxg"], self.arrays["gzg"] = gx, gz

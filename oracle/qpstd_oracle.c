@@ -591,6 +591,32 @@ static void stage_p(ctx_t *c, double *st, int t, int side, const double *obs, in
             p[i] = p[i] + s->rho[i] * vp * vp * dt *
                               (creal(c->dis0[i]) - 1.0 / 12.0 * vp * dt * vp * dt * creal(c->dis2[i]));
         }
+    } else if (s->lr_row > 0) {
+        /* low-rank form: psc = sum_a U[x][a] sum_b A[a][b] Re F^-1[Vt_b F div] / N
+         * (multv_kernel / sumlw_kernel / sumlw2_kernel, acsglw.cu:1375-1497, with
+         * the sums in double), then p += rho vp^2 dt psc -/+ dt tau aux (the
+         * dormant addsa_b_kernel, acsglw.cu:1542-1571, for the pressure term) */
+        const int row = s->lr_row, col = s->lr_col;
+        memcpy(c->dis1, c->dis0, sizeof(cplx) * (size_t)c->N);
+        fft2_exec(&c->f, c->dis1, -1);
+        double *pst = calloc((size_t)col * c->N, 8);
+        for (int b = 0; b < row; b++) {
+            const double *vt = s->lr_Vt + (size_t)b * c->N;
+            for (int i = 0; i < c->N; i++) c->dis2[i] = c->dis1[i] * vt[i] / Nd;
+            fft2_exec(&c->f, c->dis2, +1);
+#pragma omp parallel for
+            for (int i = 0; i < c->N; i++)
+                for (int a = 0; a < col; a++) pst[(size_t)a * c->N + i] += s->lr_A[a * row + b] * creal(c->dis2[i]);
+        }
+        const double sg = (kind == ORC_VAPS) ? -1.0 : +1.0;
+#pragma omp parallel for
+        for (int i = 0; i < c->N; i++) {
+            double psc = 0.0;
+            for (int a = 0; a < col; a++) psc += s->lr_U[(size_t)i * col + a] * pst[(size_t)a * c->N + i];
+            const double vp = s->vp[i];
+            p[i] = p[i] + s->rho[i] * vp * vp * dt * psc + sg * dt * s->tao[i] * aux[i];
+        }
+        free(pst);
     } else {
         memcpy(c->dis1, c->dis0, sizeof(cplx) * (size_t)c->N);
         fft2_exec(&c->f, c->dis1, -1);

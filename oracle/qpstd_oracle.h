@@ -71,6 +71,15 @@ typedef struct {
     double etas, etar;        /* Q-RTM stabilisation (scaled by 1e-6 inside) */
     double taoc;              /* Q-RTM filter tau (max tau over the window) */
     int snaps;                /* RTM checkpoints */
+    /* Low-rank form of the constant-Q pressure update (lr_row > 0; vaps / qrtm):
+     * p += rho vp^2 dt W{div} -/+ dt tau aux, with W{div} = sum_a U[x][a]
+     * sum_b A[a][b] Re F^-1[Vt_b F div] / N, the operator of the reference's
+     * dormant kernels (sgpstd-qmodeling/acsglw.cu:1375-1497) fed as its dormant
+     * pressure update does (addsa_b_kernel, acsglw.cu:1542-1571). */
+    int lr_row, lr_col;
+    const double *lr_U;       /* nxx*nzz x lr_col */
+    const double *lr_Vt;      /* lr_row x nxx*nzz: the half-grid factors mirrored to the full grid */
+    const double *lr_A;       /* lr_col x lr_row */
 } orc_shot;
 
 /* Forward modeling (aps / vaps).  gather: nt*nr time-major, p after the
