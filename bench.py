@@ -394,13 +394,13 @@ def main():
     if args.form == "lowrank":
         if kname not in ("vaps", "qrtm"):
             raise SystemExit("--form lowrank applies to the constant-Q workloads (vaps2, qrtm4)")
-        rank = 5 if kname == "qrtm" else 4
+        lr_rank = 5 if kname == "qrtm" else 4
         t_dec = time.perf_counter()
-        factors = qpstd.lowrank_factors(shots, rank)
+        factors = qpstd.lowrank_factors(shots, lr_rank)
         t_dec = time.perf_counter() - t_dec
         for i, f in enumerate(factors):
             qpstd.shot_set_lowrank(B.shot(i), f)
-        desc = dict(desc, form=f"low-rank, rank {rank} (host FP64 decomposition of every window: {t_dec:.1f} s, "
+        desc = dict(desc, form=f"low-rank, rank {lr_rank} (host FP64 decomposition of every window: {t_dec:.1f} s, "
                                f"untimed setup)")
     streams = [torch.cuda.ExternalStream(p) for p in B.stream_ptrs()]
     flush = None
