@@ -293,41 +293,57 @@ template <int RMAX> struct RtFFT {
     }
 };
 
-// Compile-time Stockham passes (NS = product of the earlier radices).
-template <int S, int M, int NS, int R, int... Rest>
+// Compile-time Stockham passes (NS = product of the earlier radices).  TX = 0:
+// one butterfly per thread (the CTA has at least m / R threads per line for
+// every pass); TX > 0: the line has TX threads and a pass of B = m / R
+// butterflies gives thread j the butterflies j, j + TX, ... (NB = ceil(B / TX)
+// of them), all loaded before the pass's barrier, so NB * R <= 16 keeps them
+// in registers.  That is how lines longer than 768 butterflies of the smallest
+// radix (m above about 5000) stay in one CTA.
+template <int S, int M, int NS, int TX, int R, int... Rest>
 __device__ __forceinline__ void ct_passes(float2* line, const float2* __restrict__ tw, bool lact) {
     constexpr int B = M / R;
-    const int j = threadIdx.x;
-    const bool act = lact && (j < B);
-    float2 v[R];
-    int k = 0;
-    if (act) {
-        if constexpr (NS > 1) k = j % NS;
+    constexpr int NB = (TX == 0) ? 1 : (B + TX - 1) / TX;
+    static_assert(NB * R <= 16, "butterflies of one thread must fit its registers");
+    float2 v[NB][R];
+    int k[NB];
 #pragma unroll
-        for (int r = 0; r < R; r++) v[r] = line[j + r * B];
-        if constexpr (NS > 1) {
-            float2 w1 = __ldg(&tw[k * (M / (NS * R))]);
-            if (S > 0) w1.y = -w1.y;
-            float2 w = w1;
+    for (int q = 0; q < NB; q++) {
+        const int j = threadIdx.x + q * TX;
+        k[q] = 0;
+        if (lact && j < B) {
+            if constexpr (NS > 1) k[q] = j % NS;
 #pragma unroll
-            for (int r = 1; r < R; r++) {
-                v[r] = cmul(v[r], w);
-                w = cmul(w, w1);
+            for (int r = 0; r < R; r++) v[q][r] = line[j + r * B];
+            if constexpr (NS > 1) {
+                float2 w1 = __ldg(&tw[k[q] * (M / (NS * R))]);
+                if (S > 0) w1.y = -w1.y;
+                float2 w = w1;
+#pragma unroll
+                for (int r = 1; r < R; r++) {
+                    v[q][r] = cmul(v[q][r], w);
+                    w = cmul(w, w1);
+                }
             }
+            dft<R, S>(v[q]);
         }
-        dft<R, S>(v);
     }
     __syncthreads();
-    if (act) {
-        const int base = (j - k) * R + k;
 #pragma unroll
-        for (int r = 0; r < R; r++) line[base + r * NS] = v[r];
+    for (int q = 0; q < NB; q++) {
+        const int j = threadIdx.x + q * TX;
+        if (lact && j < B) {
+            const int base = (j - k[q]) * R + k[q];
+#pragma unroll
+            for (int r = 0; r < R; r++) line[base + r * NS] = v[q][r];
+        }
     }
     __syncthreads();
-    if constexpr (sizeof...(Rest) > 0) ct_passes<S, M, NS * R, Rest...>(line, tw, lact);
+    if constexpr (sizeof...(Rest) > 0) ct_passes<S, M, NS * R, TX, Rest...>(line, tw, lact);
 }
 
-template <int... Rs> struct CtFFT {
+template <int TX, int... Rs> struct CtFFTX {
+    static constexpr int kTX = TX;  // threads per line (0: one butterfly each)
     static constexpr int kNst = sizeof...(Rs);
     static constexpr int kRad[kNst] = {Rs...};
     static constexpr int M = (Rs * ...);
@@ -337,16 +353,17 @@ template <int... Rs> struct CtFFT {
         return r;
     }();
     template <int S> __device__ __forceinline__ static void run(float2* buf, int ld, const FFTCtx& c, int L) {
-        ct_passes<S, M, 1, Rs...>(buf + threadIdx.y * ld, c.w, threadIdx.y < L);
+        ct_passes<S, M, 1, TX, Rs...>(buf + threadIdx.y * ld, c.w, threadIdx.y < L);
     }
-    // host: is p exactly this plan?
+    // host: is p exactly this plan (radices and, for TX > 0, threads per line)?
     static bool matches(const FFTPlanDev& p) {
-        if (p.m != M || p.nst != kNst) return false;
+        if (p.m != M || p.nst != kNst || (TX > 0 && p.tx != TX)) return false;
         for (int i = 0; i < kNst; i++)
             if (p.pass[i].R != kRad[i]) return false;
         return true;
     }
 };
+template <int... Rs> using CtFFT = CtFFTX<0, Rs...>;
 
 // A list of compiled plans and its dispatch: first_match calls fn(Policy{})
 // with the first listed plan that p equals and returns true, else false.

@@ -224,9 +224,71 @@ static void host_fft(std::vector<std::complex<double>>& x, const std::vector<int
     if (src != &x) x = *src;
 }
 
-int build_plan_host(int n, HostPlan& hp) {
+// Lengths whose x passes are compiled with the plan built in (xplans_list.h):
+// their passes run about a fifth faster than the run-time plan (measured on
+// the z passes), which the planner counts as a lower cost.  Long entries
+// (TX > 0) are the only plans for lines beyond the one-butterfly-per-thread
+// limit.
+struct CompiledPlan {
+    int tx;
+    std::vector<int> rad;
+    int m() const {
+        int v = 1;
+        for (int r : rad) v *= r;
+        return v;
+    }
+};
+#define QP_XPLAN_ENTRY(TX, ...) CompiledPlan{TX, {__VA_ARGS__}},
+static const std::vector<CompiledPlan>& compiled_plans() {
+    static const std::vector<CompiledPlan> v = {QP_XPLANS_ALL(QP_XPLAN_ENTRY)};
+    return v;
+}
+static const CompiledPlan* compiled_length(int m) {
+    for (const CompiledPlan& c : compiled_plans())
+        if (c.m() == m) return &c;
+    return nullptr;
+}
+static bool compiled_conv_length(int m) {
+    const CompiledPlan* c = compiled_length(m);
+    return c && c->tx == 0;
+}
+
+// The smooth lengths m in [2n-1, 2.3n+8] a zero-padded convolution or a
+// Bluestein transform of an n-point line can use, with their radices: the
+// cheapest by pass work (extra_pass: 1 for Bluestein's two transforms per
+// DFT), compiled plans counted at 0.8; with allow_long, a compiled long plan
+// when no length has a one-butterfly-per-thread plan.
+static bool choose_inner_length(int n, bool allow_long, int extra_pass, HostPlan& hp) {
+    double best = 1e300;
+    for (int m = 2 * n - 1; m <= (int)(2.3 * n) + 8; m++) {
+        if (!smooth7(m)) continue;
+        std::vector<int> r;
+        if (!factor_direct(m, r)) continue;
+        double cost = (double)m * (r.size() + extra_pass) * radix_weight(r);
+        if (compiled_conv_length(m)) cost *= 0.8;
+        if (cost < best) {
+            best = cost;
+            hp.m = m;
+            hp.rad = r;
+            hp.tx = 0;
+        }
+    }
+    if (best < 1e300 || !allow_long) return best < 1e300;
+    for (int m = 2 * n - 1; m <= (int)(2.3 * n) + 8; m++) {
+        const CompiledPlan* c = compiled_length(m);
+        if (!c || c->tx == 0) continue;
+        hp.m = m;
+        hp.rad = c->rad;
+        hp.tx = c->tx;
+        return true;
+    }
+    return false;
+}
+
+int build_plan_host(int n, HostPlan& hp, bool allow_long) {
     hp.n = n;
     hp.blue = 0;
+    hp.tx = 0;
     if (n == 1) {
         hp.m = 1;
         hp.rad.clear();
@@ -234,21 +296,17 @@ int build_plan_host(int n, HostPlan& hp) {
         hp.m = n;
     } else {
         // Bluestein: the {2,3,5,7}-smooth inner length in [2n-1, 2.3n] with the
-        // lowest pass work, m * (passes + 1), weighted by radix_weight
+        // lowest pass work, m * (passes + 1), weighted by radix_weight; for long
+        // lines the compiled long plan the convolution plan of n takes too
         hp.blue = 1;
-        double best = 1e300;
-        for (int m = 2 * n - 1; m <= (int)(2.3 * n) + 8; m++) {
-            if (!smooth7(m)) continue;
-            std::vector<int> r;
-            if (!factor_direct(m, r)) continue;
-            const double cost = (double)m * (r.size() + 1) * radix_weight(r);
-            if (cost < best) {
-                best = cost;
-                hp.m = m;
-                hp.rad = r;
-            }
+        if (!choose_inner_length(n, allow_long, 1, hp)) return -1;
+        if (hp.tx > 0) {
+            HostPlan c;
+            if (build_conv_plan_host(n, c, true) || c.tx == 0) return -1;
+            hp.m = c.m;
+            hp.rad = c.rad;
+            hp.tx = c.tx;
         }
-        if (best == 1e300) return -1;
     }
     const int m = hp.m;
     hp.w.resize(m);
@@ -280,43 +338,14 @@ int build_plan_host(int n, HostPlan& hp) {
 // one zero-padded forward and one inverse length-m FFT (every lag i-j in
 // (-n, n) lands on a distinct slot of the length-m wrap), so a window length
 // with a large prime factor costs two smooth FFTs instead of Bluestein's four.
-// Lengths whose convolution passes are compiled with the plan built in
-// (xplans_list.h): their passes run about a fifth faster than the run-time plan
-// (measured on the z passes), which the planner counts as a lower cost.
-#define QP_XPLAN_PRODUCT(...) qp_product({__VA_ARGS__}),
-static int qp_product(std::initializer_list<int> r) {
-    int m = 1;
-    for (int x : r) m *= x;
-    return m;
-}
-static bool compiled_conv_length(int m) {
-    static const int lens[] = {QP_XPLANS_ALL(QP_XPLAN_PRODUCT)};
-    for (int x : lens)
-        if (x == m) return true;
-    return false;
-}
-
-int build_conv_plan_host(int n, HostPlan& hp) {
+int build_conv_plan_host(int n, HostPlan& hp, bool allow_long) {
     hp = HostPlan();
     hp.n = n;
     if (n == 1 || factor_direct(n, hp.rad)) {
         hp.m = (n == 1) ? 1 : n;
         if (n == 1) hp.rad.clear();
-    } else {
-        double best = 1e300;
-        for (int m = 2 * n - 1; m <= (int)(2.3 * n) + 8; m++) {
-            if (!smooth7(m)) continue;
-            std::vector<int> r;
-            if (!factor_direct(m, r)) continue;
-            double cost = (double)m * r.size() * radix_weight(r);
-            if (compiled_conv_length(m)) cost *= 0.8;
-            if (cost < best) {
-                best = cost;
-                hp.m = m;
-                hp.rad = r;
-            }
-        }
-        if (best == 1e300) return -1;
+    } else if (!choose_inner_length(n, allow_long, 0, hp)) {
+        return -1;
     }
     hp.w.resize(hp.m);
     for (int k = 0; k < hp.m; k++) {
@@ -367,8 +396,12 @@ int fill_plan_dev(const HostPlan& hp, FFTPlanDev& d) {
         maxb = std::max(maxb, p.B);
         ns *= p.R;
     }
-    d.tx = std::min(QP_MAXTHREADS, (maxb + 31) / 32 * 32);
     d.w = d.chirp = d.bhat = nullptr;
+    if (hp.tx > 0) {  // a compiled long plan: TX threads, several butterflies each
+        d.tx = hp.tx;
+        return 0;
+    }
+    d.tx = std::min(QP_MAXTHREADS, (maxb + 31) / 32 * 32);
     return (maxb > QP_MAXTHREADS) ? -1 : 0;
 }
 

@@ -21,13 +21,16 @@ void shift_symbols(int n, double d, int which, std::vector<std::complex<double>>
 
 struct HostPlan {
     int n = 0, m = 0, blue = 0;
+    int tx = 0;  // threads per line of a compiled long plan (0: one butterfly per thread)
     std::vector<int> rad;
     std::vector<std::complex<double>> w, chirp, bhat;
 };
-int build_plan_host(int n, HostPlan& hp);
+// allow_long: lines that only a compiled long plan (xplans_list.h, group 3)
+// can run may use one; only the x passes have those kernels.
+int build_plan_host(int n, HostPlan& hp, bool allow_long = false);
 // Length-m FFT plan for separable operators applied as zero-padded circular
 // convolutions (m = n when n factors into radices <= 16, else smooth m >= 2n-1).
-int build_conv_plan_host(int n, HostPlan& hp);
+int build_conv_plan_host(int n, HostPlan& hp, bool allow_long = false);
 // Length-m multiplier of the convolution form of the symbol Hn (1/n folded in).
 void conv_table(const HostPlan& hp, const std::vector<std::complex<double>>& Hn,
                 std::vector<std::complex<double>>& out);

@@ -141,8 +141,9 @@ int collect(Req& r) {
 // Admit r if memory allows; returns 1 admitted, 0 not now, < 0 failed.
 int admit(qpstd_server* sv, Req& r, bool alone) {
     qpstd_shot_desc d = r.d;
-    // windows whose transforms the fused passes cannot plan (lines longer than
-    // one CTA covers, about 2600 points) run in the plain cuFFT form
+    // windows whose transforms the fused passes cannot plan (x lines beyond the
+    // compiled long plans, about 4600 points; z lines beyond about 2800) run in
+    // the plain cuFFT form
     if (qpstd_shot_bytes(&d) < 0) d.method = QPSTD_PLAIN;
     r.plain = d.method == QPSTD_PLAIN;
     const size_t avail = sv->budget > sv->reserved ? sv->budget - sv->reserved : 0;

@@ -291,7 +291,7 @@ static int setup_plain(qpstd_shot* s, const qpstd_shot_desc* d) {
 // separable operators (two staggered derivatives and the k^2 term per axis).
 static int setup_conv(qpstd_shot* s, const qpstd_shot_desc* d) {
     HostPlan cx, cz;
-    if (build_conv_plan_host(d->nxx, cx) || build_conv_plan_host(d->nzz, cz))
+    if (build_conv_plan_host(d->nxx, cx, true) || build_conv_plan_host(d->nzz, cz))
         return fail(QPSTD_ENOTSUP, "no convolution plan for this length");
     int rc;
     if ((rc = upload_plan(s, cx, s->pxc))) return rc;
@@ -451,7 +451,8 @@ int shot_create_ex(const qpstd_shot_desc* d, qpstd_shot** out, bool tune, qp::Ar
     // FFT plans and tile shapes of the fused passes (the plain form uses cuFFT)
     if (d->method == QPSTD_FUSED) {
         HostPlan hx, hz;
-        if (build_plan_host(nxx, hx) || build_plan_host(nzz, hz)) return bail(fail(QPSTD_ENOTSUP, "no FFT plan for this length"));
+        if (build_plan_host(nxx, hx, true) || build_plan_host(nzz, hz))
+            return bail(fail(QPSTD_ENOTSUP, "no FFT plan for this length"));
         if ((rc = upload_plan(s, hx, s->px))) return bail(rc);
         if ((rc = upload_plan(s, hz, s->pz))) return bail(rc);
         if ((rc = setup_conv(s, d))) return bail(rc);
@@ -1038,8 +1039,8 @@ extern "C" long long qpstd_shot_bytes(const qpstd_shot_desc* d) {
     const double nr = std::max(d->nr, 1), nx = d->nxx - 2 * d->pml, nz = d->nzz - 2 * d->pml;
     const bool fused = d->method != QPSTD_PLAIN;
     HostPlan cx, cz, ex, ez;
-    if (fused && (build_conv_plan_host(d->nxx, cx) || build_conv_plan_host(d->nzz, cz) ||
-                  build_plan_host(d->nxx, ex) || build_plan_host(d->nzz, ez)))
+    if (fused && (build_conv_plan_host(d->nxx, cx, true) || build_conv_plan_host(d->nzz, cz) ||
+                  build_plan_host(d->nxx, ex, true) || build_plan_host(d->nzz, ez)))
         return -1;  // no fused plan for these lengths
     double f = (rtm ? 18.0 : 9.0) * N + 6.0 * N;                       // wavefields; div, Lz, bbx, bbz, c1, c2
     if (fused) {

@@ -4,46 +4,6 @@
 
 namespace qp {
 
-// One-time construction of the per-kz convolution multipliers (see VtabArgs).
-__global__ void __launch_bounds__(768, 1) vz_convtab_kernel(VtabArgs a) {
-    extern __shared__ float2 smem[];
-    __shared__ FFTPass s_pass[QP_MAXST];
-    __shared__ FFTPass s_pass_c[QP_MAXST];
-    const FFTCtx fe = make_ctx(a.pl, s_pass);
-    const FFTCtx fcc = make_ctx(a.plc, s_pass_c);
-    const int L = a.L, n = a.nxx, m = a.plc.m, ld = max(a.pl.m, a.plc.m);
-    const int kz = blockIdx.x * L + threadIdx.y;
-    const bool valid = kz < a.nzh;
-    float2* line = smem + threadIdx.y * ld;
-    const double kzsq = a.kz2[valid ? kz : 0];
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        const double k2 = (double)a.kx2[k] + kzsq;
-        double s;
-        if (a.sym == 4) s = a.V[(size_t)((k < a.nxh) ? k : n - k) * a.nzh + (valid ? kz : 0)];
-        else if (a.sym == 1) s = k2;
-        else if (a.sym == 0) s = pow(k2, 1.0 / 32.0);
-        else if (a.sym == 2) s = pow(k2, 33.0 / 32.0);
-        else s = pow(k2, 0.505);
-        line[k] = make_float2((float)s, 0.f);
-    }
-    __syncthreads();
-    dft_n<+1>(smem, ld, fe, L);  // sum_k s e^{+2 pi i k d/n}
-    // wrap to length m: lags 0..n-1 stay, lags -(n-1)..-1 go to m-n+1..m-1 (m >= 2n-1)
-    if (m > n) {
-        for (int dd = 1 + threadIdx.x; dd < n; dd += blockDim.x) line[m - dd] = line[n - dd];
-        __syncthreads();
-        for (int k = n + threadIdx.x; k <= m - n; k += blockDim.x) line[k] = make_float2(0.f, 0.f);
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < m; k += blockDim.x) line[k] = make_float2(line[k].x * a.norm, 0.f);
-    __syncthreads();
-    fft_m<-1>(smem, ld, fcc, L);
-    // the wrapped kernel is even, so its transform is real and even: keep 0..m/2
-    const int mh = m / 2 + 1;
-    if (valid)
-        for (int k = threadIdx.x; k < mh; k += blockDim.x) a.out[(size_t)kz * mh + k] = line[k].x / (float)m;
-}
-
 // ---- launchers -------------------------------------------------------------------
 static size_t lsm(int L, int m, int nbuf) { return sizeof(float2) * (size_t)nbuf * L * m; }
 static int zgrid(int nxx, int L) { return (nxx + 2 * L - 1) / (2 * L); }
@@ -66,6 +26,7 @@ void launch_vz_passA(const VzArgsA& a, cudaStream_t s) {
 void launch_vz_xspec(const VxsArgs& a, cudaStream_t s) {
     const int grid = (a.nzh + a.L - 1) / a.L;
     const size_t sm = lsm(a.L, a.pl.m, a.mode == 0 ? 2 : 1);
+    if (xplan_launch_xspec(a, s, dim3(grid), dim3(a.pl.tx, a.L), sm)) return;  // a compiled long plan
     if (plan_max_radix(a.pl) <= 12) vz_xspec_kernel<RtFFT<12>><<<grid, dim3(a.pl.tx, a.L), sm, s>>>(a);
     else vz_xspec_kernel<RtFFT<16>><<<grid, dim3(a.pl.tx, a.L), sm, s>>>(a);
 }
@@ -80,12 +41,17 @@ void launch_vz_xspec_conv(const VxsArgs& a, cudaStream_t s) {
     else vz_xspec_conv_kernel<1, RtFFT<16>><<<grid, blk, lsm(a.L, a.plc.m, 1), s>>>(a);
 }
 void launch_vz_convtab(const VtabArgs& a, cudaStream_t s) {
-    vz_convtab_kernel<<<(a.nzh + a.L - 1) / a.L, dim3(max(a.pl.tx, a.plc.tx), a.L), lsm(a.L, max(a.pl.m, a.plc.m), 1), s>>>(a);
+    const int grid = (a.nzh + a.L - 1) / a.L;
+    const dim3 blk(max(a.pl.tx, a.plc.tx), a.L);
+    const size_t sm = lsm(a.L, max(a.pl.m, a.plc.m), 1);
+    if (xplan_launch_convtab(a, s, dim3(grid), blk, sm)) return;  // a compiled long plan
+    vz_convtab_kernel<RtFFT<16>><<<grid, blk, sm, s>>>(a);
 }
 void launch_lr_xconv(const LrxArgs& a, cudaStream_t s) {
     const int grid = (a.nzh + a.L - 1) / a.L;
     const dim3 blk(a.plc.tx, a.L);
     const size_t sm = lsm(a.L, a.plc.m, 2);
+    if (xplan_launch_lr_xconv(a, s, dim3(grid), blk, sm)) return;  // a compiled long plan
     if (plan_max_radix(a.plc) <= 12) lr_xconv_kernel<RtFFT<12>><<<grid, blk, sm, s>>>(a);
     else lr_xconv_kernel<RtFFT<16>><<<grid, blk, sm, s>>>(a);
 }
@@ -143,7 +109,7 @@ int vz_set_smem_limits() {
     bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<3, RtFFT<16>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<1, RtFFT<12>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
     bad |= cudaFuncSetAttribute(vz_xspec_conv_kernel<1, RtFFT<16>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
-    bad |= cudaFuncSetAttribute(vz_convtab_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
+    bad |= cudaFuncSetAttribute(vz_convtab_kernel<RtFFT<16>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
     bad |= cudaFuncSetAttribute(lr_xconv_kernel<RtFFT<12>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
     bad |= cudaFuncSetAttribute(lr_xconv_kernel<RtFFT<16>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess;
     return bad ? -1 : 0;

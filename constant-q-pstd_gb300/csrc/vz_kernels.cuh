@@ -210,6 +210,50 @@ __global__ void __maxnreg__(NOUT == 3 ? QP_WIDE_REGS : FP::kMaxRadix <= 12 ? QP_
     }
 }
 
+// One-time construction of the per-kz convolution multipliers (see VtabArgs).
+// FP: transform policy of both plans (the run-time plan, or one compiled long
+// plan when the exact length's Bluestein plan and the convolution plan are the
+// same length, as the planner makes them for long lines).
+template <class FP>
+__global__ void __launch_bounds__(768, 1) vz_convtab_kernel(VtabArgs a) {
+    extern __shared__ float2 smem[];
+    __shared__ FFTPass s_pass[QP_MAXST];
+    __shared__ FFTPass s_pass_c[QP_MAXST];
+    const FFTCtx fe = make_ctx(a.pl, s_pass);
+    const FFTCtx fcc = make_ctx(a.plc, s_pass_c);
+    const int L = a.L, n = a.nxx, m = a.plc.m, ld = max(a.pl.m, a.plc.m);
+    const int kz = blockIdx.x * L + threadIdx.y;
+    const bool valid = kz < a.nzh;
+    float2* line = smem + threadIdx.y * ld;
+    const double kzsq = a.kz2[valid ? kz : 0];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const double k2 = (double)a.kx2[k] + kzsq;
+        double s;
+        if (a.sym == 4) s = a.V[(size_t)((k < a.nxh) ? k : n - k) * a.nzh + (valid ? kz : 0)];
+        else if (a.sym == 1) s = k2;
+        else if (a.sym == 0) s = pow(k2, 1.0 / 32.0);
+        else if (a.sym == 2) s = pow(k2, 33.0 / 32.0);
+        else s = pow(k2, 0.505);
+        line[k] = make_float2((float)s, 0.f);
+    }
+    __syncthreads();
+    dft_n<+1, FP>(smem, ld, fe, L);  // sum_k s e^{+2 pi i k d/n}
+    // wrap to length m: lags 0..n-1 stay, lags -(n-1)..-1 go to m-n+1..m-1 (m >= 2n-1)
+    if (m > n) {
+        for (int dd = 1 + threadIdx.x; dd < n; dd += blockDim.x) line[m - dd] = line[n - dd];
+        __syncthreads();
+        for (int k = n + threadIdx.x; k <= m - n; k += blockDim.x) line[k] = make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < m; k += blockDim.x) line[k] = make_float2(line[k].x * a.norm, 0.f);
+    __syncthreads();
+    fft_m<-1, FP>(smem, ld, fcc, L);
+    // the wrapped kernel is even, so its transform is real and even: keep 0..m/2
+    const int mh = m / 2 + 1;
+    if (valid)
+        for (int k = threadIdx.x; k < mh; k += blockDim.x) a.out[(size_t)kz * mh + k] = line[k].x / (float)m;
+}
+
 // ---- z pass B -----------------------------------------------------------------
 template <class FP>
 __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz_passB_kernel(VzArgsB a) {

@@ -189,7 +189,8 @@ long long qpstd_shot_bytes(const qpstd_shot_desc *d);
  * largest revolve snapshot count, up to its d->snaps, that fits at admission;
  * the image is the one qpstd_rtm_shot gives with that count (qpstd_server_status
  * reports it).  A fused request whose window the fused passes cannot plan
- * (lines longer than one CTA covers, about 2600 points) runs in the plain form. */
+ * (x lines beyond about 4600 points, z lines beyond about 2800) runs in the
+ * plain form. */
 typedef struct qpstd_server qpstd_server;
 int qpstd_server_create(long long mem_budget, int max_active, qpstd_server **out);
 /* Waits for every submitted request, then stops the worker. */

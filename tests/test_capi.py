@@ -52,6 +52,9 @@ def test_shot_bytes_grows_by_the_snapshot_pool():
 
 def test_shot_bytes_marks_windows_the_fused_passes_cannot_plan():
     import workloads as W
+    # x lines up to about 4600 points plan (compiled long plans); 6000 do not
     d = W.make_shot(qpstd.APS, 4096, 24, 10, 40, 0.0005, 25.0, seed=9)
+    assert qpstd.shot_bytes(d) > 0
+    d = W.make_shot(qpstd.APS, 6000, 24, 10, 40, 0.0005, 25.0, seed=9)
     assert qpstd.shot_bytes(d) == -1
     assert qpstd.shot_bytes(dict(d, method=qpstd.PLAIN)) > 0
