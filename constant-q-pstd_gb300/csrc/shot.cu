@@ -1414,6 +1414,17 @@ __global__ void filter_image_kernel(int nx, int nz, float rdx2, float rdz2, cons
     out[i] = (img[i + 1] + img[i - 1] - 2.f * img[i]) * rdz2 + (img[i + nz] + img[i - nz] - 2.f * img[i]) * rdx2;
 }
 
+extern "C" int qpstd_pml_profiles(int pml, float fd, int nxx, int nzz, float dx, float dz, float dt, float* out) {
+    if (pml < 2 || nxx < 2 * pml + 1 || nzz < 2 * pml + 1 || !out) return fail(QPSTD_EINVAL, "bad CPML grid");
+    std::vector<double> v[8];  // i_ax, i_bx, i_az, i_bz, h_ax, h_bx, h_az, h_bz
+    pml_coeffs(pml, fd, nxx, nzz, dx, dz, dt, v);
+    const int order[8] = {0, 1, 4, 5, 2, 3, 6, 7};  // x tables, then z tables
+    size_t q = 0;
+    for (int k : order)
+        for (double x : v[k]) out[q++] = (float)x;
+    return QPSTD_OK;
+}
+
 extern "C" int qpstd_filter_image(int nx, int nz, float dx, float dz, const float* img, float* imgf) {
     if (nx < 1 || nz < 1 || !img || !imgf) return fail(QPSTD_EINVAL, "bad filter arguments");
     const size_t n = (size_t)nx * nz;

@@ -78,6 +78,7 @@ EXPORTS = {
     "qpstd_shot_profile_read": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
     "qpstd_shot_info": (C.c_longlong, [C.c_void_p, C.c_int]),
     "qpstd_shot_set_lowrank": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _fp, _fp, _dp]),
+    "qpstd_pml_profiles": (C.c_int, [C.c_int, C.c_float, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, _fp]),
     "qpstd_batch_create": (C.c_int, [C.POINTER(ShotDesc), C.c_int, C.POINTER(C.c_void_p)]),
     "qpstd_batch_destroy": (C.c_int, [C.c_void_p]),
     "qpstd_batch_size": (C.c_int, [C.c_void_p]),

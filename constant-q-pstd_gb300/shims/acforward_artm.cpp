@@ -10,12 +10,13 @@ extern "C" void acforward(int snapnum, int GPU_N, int tmax, float dt, float *rik
                           float *h_bx, float *h_az, float *h_bz, float *kxsmr, float *kxscr, float *kzsmr,
                           float *kzscr, float *kxsmi, float *kxsci, float *kzsmi, float *kzsci, float *img_sp,
                           float *ssg_sp, float fobs, float v0, char fname4[40], char fname5[40], char recname[60]) {
-    (void)numprocs, (void)k2da, (void)k2d1, (void)k2d2, (void)k2d3, (void)i_ax, (void)i_az, (void)i_bz;
-    (void)h_ax, (void)h_bx, (void)h_az, (void)h_bz, (void)kxsmr, (void)kxscr, (void)kzsmr, (void)kzscr;
+    (void)numprocs, (void)k2da, (void)k2d1, (void)k2d2, (void)k2d3;
+    (void)kxsmr, (void)kxscr, (void)kzsmr, (void)kzscr;
     (void)kxsmi, (void)kxsci, (void)kzsmi, (void)kzsci;
     if (!qpshim::one_gpu(GPU_N)) return;
-    const qpshim::Common c{tmax, dt, rik, myid, gxp, gzp, nrmx, nx, nz, nxx, nzz, pml, dx, dz, sroffmx, disx,
+    qpshim::Common c{tmax, dt, rik, myid, gxp, gzp, nrmx, nx, nz, nxx, nzz, pml, dx, dz, sroffmx, disx,
                            nxt, nzt, tracenum, i_bx, fname4, fname5};
+    qpshim::set_cpml(c, i_ax, i_bx, i_az, i_bz, h_ax, h_bx, h_az, h_bz);
     float *models[8] = {vpt, rhot, bbxt, bbzt, nullptr, nullptr, nullptr, nullptr};
     qpshim::rtm(c, singpu, nshot, models, QPSTD_ARTM, snapnum, img_sp, ssg_sp, fobs, v0, 0.f, 0.f, recname);
 }

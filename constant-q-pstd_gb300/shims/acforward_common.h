@@ -69,7 +69,43 @@ struct Common {
     char *fname4, *fname5;
     float fd = 0.f;  // CPML frequency when known (the native programs); 0: recovered from i_bx
     int method = QPSTD_FUSED;
+    // the caller's CPML profiles (i_ax, i_bx, i_az, i_bz, h_ax, h_bx, h_az, h_bz), when it passes them
+    const float *cpml[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 };
+
+inline void set_cpml(Common &c, const float *i_ax, const float *i_bx, const float *i_az, const float *i_bz,
+                     const float *h_ax, const float *h_bx, const float *h_az, const float *h_bz) {
+    const float *t[8] = {i_ax, i_bx, i_az, i_bz, h_ax, h_bx, h_az, h_bz};
+    for (int k = 0; k < 8; k++) c.cpml[k] = t[k];
+}
+
+// The reference's acforward takes every coefficient table from its caller; the
+// library computes them itself from the grid, dt and the CPML frequency.  Warns
+// (stderr) when the caller's CPML profiles differ from the library's by more
+// than 1e-4 of their largest value, i.e. when a modified main passes tables of
+// another CPML, which the library would not apply.
+inline void check_cpml(const Common &c, float fd) {
+    if (!c.cpml[0]) return;
+    std::vector<float> lib((size_t)4 * (c.nxx + c.nzz));
+    if (qpstd_pml_profiles(c.pml, fd, c.nxx, c.nzz, c.dx, c.dz, c.dt, lib.data()) != QPSTD_OK) return;
+    const char *names[8] = {"i_ax", "i_bx", "i_az", "i_bz", "h_ax", "h_bx", "h_az", "h_bz"};
+    const int at[8] = {0, 1, 4, 5, 2, 3, 6, 7};  // positions in qpstd_pml_profiles' order
+    for (int k = 0; k < 8; k++) {
+        const bool x = (k == 0 || k == 1 || k == 4 || k == 5);
+        const int n = x ? c.nxx : c.nzz;
+        const size_t off = (at[k] < 4) ? (size_t)at[k] * c.nxx : (size_t)4 * c.nxx + (size_t)(at[k] - 4) * c.nzz;
+        double dmax = 0.0, vmax = 0.0;
+        for (int i = 0; i < n; i++) {
+            dmax = std::max(dmax, std::fabs((double)c.cpml[k][i] - lib[off + i]));
+            vmax = std::max(vmax, std::fabs((double)lib[off + i]));
+        }
+        if (dmax > 1e-4 * std::max(vmax, 1e-30))
+            fprintf(stderr,
+                    "warning: the %s table passed to acforward differs from the CPML profile libqpstd applies "
+                    "(max difference %.3g of %.3g); the library uses get_pml_parameters with pml=%d, fd=%g\n",
+                    names[k], dmax, vmax, c.pml, fd);
+    }
+}
 
 // One shot on its window (sgpstd-qmodeling/acps4.cu:312-430).
 struct Shot {
@@ -255,6 +291,7 @@ inline int model_with_snapshots(const Common &c, const Shot &s, const qpstd_shot
 inline void model(const Common &c, MultiGPU *singpu, int nshot, float *const *models, int kind, int flagout,
                   const char *recpre, const char *snappre) {
     const float fd = cpml_fd(c);
+    check_cpml(c, fd);
     AsyncWriter wr;
     for (int ns = 0; ns < nshot; ns++) {
         Shot s;
@@ -325,6 +362,7 @@ inline int rtm_accumulate(const Common &c, const Shot &s, const float *img, cons
 inline void rtm(const Common &c, MultiGPU *singpu, int nshot, float *const *models, int kind, int snapnum,
                 float *img_sp, float *ssg_sp, float fobs, float v0, float etas, float etar, const char *recname) {
     const RtmArgs a{kind, snapnum, fobs, v0, etas, etar, recname};
+    check_cpml(c, cpml_fd(c));
     const size_t NI = (size_t)c.nx * c.nz;
     std::vector<float> img(NI), ssg(NI), obs;
     for (int ns = 0; ns < nshot; ns++) {

@@ -87,6 +87,13 @@ int qpstd_rtm_shot(const qpstd_shot_desc *d, const float *obs, float *img, float
  * writes are not reproduced).  img, imgf: host nx*nz. */
 int qpstd_filter_image(int nx, int nz, float dx, float dz, const float *img, float *imgf);
 
+/* The CPML profiles the library applies for a grid (get_pml_parameters,
+ * sgpstd-qmodeling/funca.c:223-340, evaluated in double and rounded): out holds
+ * i_ax, i_bx, h_ax, h_bx (nxx each), then i_az, i_bz, h_az, h_bz (nzz each).
+ * Host only.  The acforward shims compare the tables their caller computed with
+ * these and warn when they differ (the library always applies its own). */
+int qpstd_pml_profiles(int pml, float fd, int nxx, int nzz, float dx, float dz, float dt, float *out);
+
 /* Source-normalised imaging condition out = img / (ssg + sigma2) on the
  * device (host nx*nz arrays): the reference leaves this step to the user after
  * summing img_sp / ssg_sp; sigma2 is the stabilisation (e.g. 1e-26). */

@@ -58,3 +58,22 @@ def test_shot_bytes_marks_windows_the_fused_passes_cannot_plan():
     d = W.make_shot(qpstd.APS, 6000, 24, 10, 40, 0.0005, 25.0, seed=9)
     assert qpstd.shot_bytes(d) == -1
     assert qpstd.shot_bytes(dict(d, method=qpstd.PLAIN)) > 0
+
+
+def test_pml_profiles_match_the_oracle():
+    """qpstd_pml_profiles (the tables the library applies; the acforward shims
+    warn when their caller's differ) against the FP64 oracle's restatement of
+    get_pml_parameters."""
+    import numpy as np
+
+    import oracle as O
+    nxx, nzz, pml = 139, 97, 20
+    out = np.zeros(4 * (nxx + nzz), dtype=np.float32)
+    assert qpstd.lib().qpstd_pml_profiles(pml, 20.0, nxx, nzz, 10.0, 12.0, 0.001, out.ctypes.data_as(qpstd._fp)) == 0
+    ref = O.pml_coeffs(pml, 20.0, nxx, nzz, 10.0, 12.0, 0.001)
+    order = ["i_ax", "i_bx", "h_ax", "h_bx", "i_az", "i_bz", "h_az", "h_bz"]
+    q = 0
+    for name in order:
+        n = nxx if name.endswith("x") else nzz
+        assert np.allclose(out[q:q + n], ref[name], rtol=1e-6, atol=1e-7), name
+        q += n
