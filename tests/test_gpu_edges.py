@@ -110,8 +110,8 @@ def test_bad_shots_return_a_status(bad, msg):
         d = dict(d, gzg=np.full_like(d["gzg"], -1))
     elif bad == "snaps":
         d = dict(small_shot(qpstd.ARTM, nx=57, nz=33, nt=20), snaps=65)
-    else:  # padded width 4117: longer than one CTA's line in the fused form
-        d = W.make_shot(qpstd.APS, 4096, 24, 10, 20, 0.0005, 25.0, seed=9)
+    else:  # padded width 6021: beyond the longest line the fused form plans
+        d = W.make_shot(qpstd.APS, 6000, 24, 10, 20, 0.0005, 25.0, seed=9)
     with pytest.raises(qpstd.QpstdError, match=msg):
         if bad == "snaps":
             qpstd.rtm_shot(d, np.zeros((20, d["gxg"].size), dtype=np.float32))

@@ -109,7 +109,7 @@ def test_shot_bytes_covers_the_allocation():
 
 @pytest.mark.gpu
 def test_server_serves_windows_beyond_the_fused_lines_in_plain_form():
-    d = W.make_shot(qpstd.APS, 4096, 24, 10, 40, 0.0005, 25.0, seed=9)   # padded width 4117
+    d = W.make_shot(qpstd.APS, 6000, 24, 10, 40, 0.0005, 25.0, seed=9)   # padded width 6021
     assert qpstd.shot_bytes(d) < 0 <= qpstd.shot_bytes(dict(d, method=qpstd.PLAIN))
     ref = qpstd.model_shot(d, method=qpstd.PLAIN)
     sv = qpstd.Server(max_active=2)
