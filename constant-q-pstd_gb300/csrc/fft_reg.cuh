@@ -288,8 +288,66 @@ __device__ __forceinline__ FFTCtx make_ctx(const FFTPlanDev& pl, FFTPass* s_pass
 // results agree to the last bit of the arithmetic order.
 template <int RMAX> struct RtFFT {
     static constexpr int kMaxRadix = RMAX;
+    static constexpr bool kCompiled = false;
     template <int S> __device__ __forceinline__ static void run(float2* buf, int ld, const FFTCtx& c, int L) {
         fft_m_impl<S, RMAX>(buf, ld, c.sp, c.nst, c.w, L);
+    }
+};
+
+// Hooks of the first and last pass of a compiled transform.  run_io lets the
+// first pass take its inputs from a hook instead of the line (zero padding, a
+// multiplier, another buffer) and hands the outputs of the last pass to a hook
+// (a multiplier, another buffer), which folds the sweep over the line that the
+// same operation costs beside a plain transform -- and that sweep's barrier --
+// into the pass.  The arithmetic is the same as the separate sweep's, so the
+// results agree bit for bit.  kSep: the hook reads (writes) memory other than
+// the line, so that pass needs no barrier between its loads and its stores
+// (no thread of the pass then loads what another one stores).
+struct LineIn {
+    static constexpr bool kSep = false;
+    __device__ __forceinline__ float2 load(const float2* line, int i) const { return line[i]; }
+};
+struct LineOut {
+    static constexpr bool kSep = false;
+    __device__ __forceinline__ void store(float2* line, int i, float2 v) const { line[i] = v; }
+};
+// entries [n, m) of the line read as zeros (a zero-padded convolution)
+struct ZeroPadIn {
+    static constexpr bool kSep = false;
+    int n;
+    __device__ __forceinline__ float2 load(const float2* line, int i) const {
+        return (i < n) ? line[i] : make_float2(0.f, 0.f);
+    }
+};
+// outputs times a complex multiplier H[i] (the spectrum of a convolution kernel)
+struct MulOut {
+    static constexpr bool kSep = false;
+    const float2* __restrict__ H;
+    __device__ __forceinline__ void store(float2* line, int i, float2 v) const { line[i] = cmul(v, __ldg(&H[i])); }
+};
+// outputs times an even real multiplier stored for 0..m/2 (tk[min(i, m - i)])
+struct EvenScaleOut {
+    static constexpr bool kSep = false;
+    const float* __restrict__ tk;
+    int m;
+    __device__ __forceinline__ void store(float2* line, int i, float2 v) const {
+        line[i] = cscale(v, __ldg(&tk[min(i, m - i)]));
+    }
+};
+// outputs to another buffer (dst: this thread's line there)
+struct CopyOut {
+    static constexpr bool kSep = true;
+    float2* dst;
+    __device__ __forceinline__ void store(float2*, int i, float2 v) const { dst[i] = v; }
+};
+// inputs from another buffer times an even real multiplier
+struct EvenScaleIn {
+    static constexpr bool kSep = true;
+    const float2* src;
+    const float* __restrict__ tk;
+    int m;
+    __device__ __forceinline__ float2 load(const float2*, int i) const {
+        return cscale(src[i], __ldg(&tk[min(i, m - i)]));
     }
 };
 
@@ -299,9 +357,14 @@ template <int RMAX> struct RtFFT {
 // butterflies gives thread j the butterflies j, j + TX, ... (NB = ceil(B / TX)
 // of them), all loaded before the pass's barrier, so NB * R <= 16 keeps them
 // in registers.  That is how lines longer than 768 butterflies of the smallest
-// radix (m above about 5000) stay in one CTA.
-template <int S, int M, int NS, int TX, int R, int... Rest>
-__device__ __forceinline__ void ct_passes(float2* line, const float2* __restrict__ tw, bool lact) {
+// radix (m above about 5000) stay in one CTA.  The first pass loads through
+// `in`, the last one stores through `out`.
+template <int S, int M, int NS, int TX, class In, class Out, int R, int... Rest>
+__device__ __forceinline__ void ct_passes(float2* line, const float2* __restrict__ tw, bool lact, const In& in,
+                                          const Out& out) {
+    constexpr bool kFirst = NS == 1, kLast = sizeof...(Rest) == 0;
+    static_assert(!(kFirst && kLast && In::kSep && Out::kSep), "a one-pass transform between two other buffers");
+    constexpr bool kSep = (kFirst && In::kSep) || (kLast && Out::kSep);
     constexpr int B = M / R;
     constexpr int NB = (TX == 0) ? 1 : (B + TX - 1) / TX;
     static_assert(NB * R <= 16, "butterflies of one thread must fit its registers");
@@ -314,7 +377,10 @@ __device__ __forceinline__ void ct_passes(float2* line, const float2* __restrict
         if (lact && j < B) {
             if constexpr (NS > 1) k[q] = j % NS;
 #pragma unroll
-            for (int r = 0; r < R; r++) v[q][r] = line[j + r * B];
+            for (int r = 0; r < R; r++) {
+                if constexpr (kFirst) v[q][r] = in.load(line, j + r * B);
+                else v[q][r] = line[j + r * B];
+            }
             if constexpr (NS > 1) {
                 float2 w1 = __ldg(&tw[k[q] * (M / (NS * R))]);
                 if (S > 0) w1.y = -w1.y;
@@ -328,18 +394,21 @@ __device__ __forceinline__ void ct_passes(float2* line, const float2* __restrict
             dft<R, S>(v[q]);
         }
     }
-    __syncthreads();
+    if constexpr (!kSep) __syncthreads();
 #pragma unroll
     for (int q = 0; q < NB; q++) {
         const int j = threadIdx.x + q * TX;
         if (lact && j < B) {
             const int base = (j - k[q]) * R + k[q];
 #pragma unroll
-            for (int r = 0; r < R; r++) line[base + r * NS] = v[q][r];
+            for (int r = 0; r < R; r++) {
+                if constexpr (kLast) out.store(line, base + r * NS, v[q][r]);
+                else line[base + r * NS] = v[q][r];
+            }
         }
     }
     __syncthreads();
-    if constexpr (sizeof...(Rest) > 0) ct_passes<S, M, NS * R, TX, Rest...>(line, tw, lact);
+    if constexpr (!kLast) ct_passes<S, M, NS * R, TX, In, Out, Rest...>(line, tw, lact, in, out);
 }
 
 template <int TX, int... Rs> struct CtFFTX {
@@ -352,8 +421,18 @@ template <int TX, int... Rs> struct CtFFTX {
         for (int x : {Rs...}) r = x > r ? x : r;
         return r;
     }();
+    static constexpr bool kCompiled = true;
     template <int S> __device__ __forceinline__ static void run(float2* buf, int ld, const FFTCtx& c, int L) {
-        ct_passes<S, M, 1, TX, Rs...>(buf + threadIdx.y * ld, c.w, threadIdx.y < L);
+        ct_passes<S, M, 1, TX, LineIn, LineOut, Rs...>(buf + threadIdx.y * ld, c.w, threadIdx.y < L, LineIn{},
+                                                       LineOut{});
+    }
+    // The same transform with first- and last-pass hooks (LineIn .. EvenScaleIn
+    // above).  Caller has synchronised after filling what `in` reads; ends with
+    // a barrier, the result where `out` put it.
+    template <int S, class In, class Out>
+    __device__ __forceinline__ static void run_io(float2* buf, int ld, const FFTCtx& c, int L, const In& in,
+                                                  const Out& out) {
+        ct_passes<S, M, 1, TX, In, Out, Rs...>(buf + threadIdx.y * ld, c.w, threadIdx.y < L, in, out);
     }
     // host: is p exactly this plan (radices and, for TX > 0, threads per line)?
     static bool matches(const FFTPlanDev& p) {
@@ -462,6 +541,12 @@ __device__ __forceinline__ void dft_n(float2* buf, int ld, const FFTCtx& pl, int
 template <class FP = RtFFT<16>>
 __device__ __forceinline__ void roundtrip_conv(float2* buf, int ld, const FFTCtx& pl, int L,
                                                const float2* __restrict__ Hm) {
+    if constexpr (FP::kCompiled) {
+        // zero padding folded into the first forward pass, Hm into the last
+        FP::template run_io<-1>(buf, ld, pl, L, ZeroPadIn{pl.n}, MulOut{Hm});
+        FP::template run<+1>(buf, ld, pl, L);
+        return;
+    }
     const int l = threadIdx.y;
     float2* line = buf + l * ld;
     const bool act = l < L;

@@ -53,6 +53,21 @@ __device__ __forceinline__ void zrepack(const float2* __restrict__ S, float2* li
     }
 }
 
+// zrepack as the load hook of a compiled transform's first pass (fft_reg.cuh,
+// run_io): entry k of the packed line, read straight from the half spectra.
+struct ZRepackIn {
+    static constexpr bool kSep = true;
+    const float2* __restrict__ S;
+    int nzz, nzh, xa;
+    bool has0, has1;
+    __device__ __forceinline__ float2 load(const float2*, int k) const {
+        const int kk = (k < nzh) ? k : nzz - k;
+        const float2 A = has0 ? S[(size_t)xa * nzh + kk] : make_float2(0.f, 0.f);
+        const float2 B = has1 ? S[(size_t)(xa + 1) * nzh + kk] : make_float2(0.f, 0.f);
+        return (k < nzh) ? make_float2(A.x - B.y, A.y + B.x) : make_float2(A.x + B.y, -A.y + B.x);
+    }
+};
+
 // half spectra of rows (xa, xa+1) <- this thread's transformed packed line
 __device__ __forceinline__ void zunpack(const float2* line, float2* __restrict__ S, int nzz, int nzh, bool has0,
                                         bool has1, int xa) {

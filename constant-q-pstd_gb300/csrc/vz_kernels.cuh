@@ -23,6 +23,24 @@
 
 namespace qp {
 
+// this thread's packed line <- the inverse z transform of the half spectra S
+// of rows (xa, xa+1).  The caller has synchronised since the line was last
+// read; ends with a barrier.  With a compiled plan that is not Bluestein the
+// repacking is the first pass's load (no sweep through shared memory first).
+template <class FP>
+__device__ __forceinline__ void zrepack_inverse(const float2* __restrict__ S, float2* smem, int ld, const FFTCtx& fc,
+                                                int L, int nzz, int nzh, bool has0, bool has1, int xa) {
+    if constexpr (FP::kCompiled) {
+        if (!fc.blue) {
+            FP::template run_io<+1>(smem, ld, fc, L, ZRepackIn{S, nzz, nzh, xa, has0, has1}, LineOut{});
+            return;
+        }
+    }
+    zrepack(S, smem + threadIdx.y * ld, nzz, nzh, has0, has1, xa);
+    __syncthreads();
+    dft_n<+1, FP>(smem, ld, fc, L);
+}
+
 #define ZPASS_SETUP                                                  \
     extern __shared__ float2 smem[];                                 \
     __shared__ FFTPass s_pass[QP_MAXST];                             \
@@ -49,9 +67,7 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz
     const size_t r0 = (size_t)xa * nzz, r1 = r0 + nzz;
     const int nzh = a.nzh;
     if (a.aux_spec) {
-        zrepack(a.aux_spec, line, nzz, nzh, has0, has1, xa);
-        __syncthreads();
-        dft_n<+1, FP>(smem, ld, fc, L);
+        zrepack_inverse<FP>(a.aux_spec, smem, ld, fc, L, nzz, nzh, has0, has1, xa);
         for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
             const float2 v = line[k];
             if (has0) a.aux[r0 + k] = v.x;
@@ -181,22 +197,38 @@ __global__ void __maxnreg__(NOUT == 3 ? QP_WIDE_REGS : FP::kMaxRadix <= 12 ? QP_
         const int kz = kz0 + c;
         smem[c * ld + ix] = (kz < nzh) ? a.in[(size_t)ix * nzh + kz] : make_float2(0.f, 0.f);
     }
-    for (int k = nxx + threadIdx.x; k < m; k += blockDim.x) line[k] = make_float2(0.f, 0.f);
+    if constexpr (!FP::kCompiled)
+        for (int k = nxx + threadIdx.x; k < m; k += blockDim.x) line[k] = make_float2(0.f, 0.f);
     __syncthreads();
-    fft_m<-1, FP>(smem, ld, fc, L);
     const int kz = min(kz0 + (int)threadIdx.y, nzh - 1);
-    if (nout == 3) {
-        for (int k = threadIdx.x; k < m; k += blockDim.x) X[threadIdx.y * ld + k] = line[k];
-        __syncthreads();
-    }
     // the multipliers are even in k: rows hold entries 0..m/2
     const int mh = m / 2 + 1;
+    if constexpr (FP::kCompiled) {
+        // zero padding in the first pass; the last pass either keeps the
+        // spectrum in X (three outputs) or applies the one multiplier
+        if (nout == 3)
+            FP::template run_io<-1>(smem, ld, fc, L, ZeroPadIn{nxx}, CopyOut{X + threadIdx.y * ld});
+        else
+            FP::template run_io<-1>(smem, ld, fc, L, ZeroPadIn{nxx}, EvenScaleOut{a.tab0 + (size_t)kz * mh, m});
+    } else {
+        fft_m<-1, FP>(smem, ld, fc, L);
+        if (nout == 3) {
+            for (int k = threadIdx.x; k < m; k += blockDim.x) X[threadIdx.y * ld + k] = line[k];
+            __syncthreads();
+        }
+    }
     auto output = [&](const float* __restrict__ tab, float2* out) {
         const float2* src = (nout == 3) ? X + threadIdx.y * ld : line;
         const float* tk = tab + (size_t)kz * mh;
-        for (int k = threadIdx.x; k < m; k += blockDim.x) line[k] = cscale(src[k], __ldg(&tk[min(k, m - k)]));
-        __syncthreads();
-        fft_m<+1, FP>(smem, ld, fc, L);
+        if constexpr (FP::kCompiled) {
+            // three outputs: the multiplier is applied as the first inverse pass loads X
+            if (nout == 3) FP::template run_io<+1>(smem, ld, fc, L, EvenScaleIn{src, tk, m}, LineOut{});
+            else FP::template run<+1>(smem, ld, fc, L);
+        } else {
+            for (int k = threadIdx.x; k < m; k += blockDim.x) line[k] = cscale(src[k], __ldg(&tk[min(k, m - k)]));
+            __syncthreads();
+            fft_m<+1, FP>(smem, ld, fc, L);
+        }
         for (int g = t0; g < tot; g += nthr) {
             const int c = g & (L - 1), ix = g >> lg;
             if (kz0 + c < nzh) out[(size_t)ix * nzh + kz0 + c] = smem[c * ld + ix];
@@ -262,9 +294,7 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz
     float2* acc = smem + (size_t)(L + threadIdx.y) * ld;  // running total of this line pair
     // three terms, written out in sequence (a loop here costs register spills)
     auto term = [&](const float2* spec, const float* cf, float sg, bool first) {
-        zrepack(spec, line, nzz, nzh, has0, has1, xa);
-        __syncthreads();
-        dft_n<+1, FP>(smem, ld, fc, L);
+        zrepack_inverse<FP>(spec, smem, ld, fc, L, nzz, nzh, has0, has1, xa);
         for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
             const float2 y = line[k];
             float2 t = first ? make_float2(0.f, 0.f) : acc[k];
@@ -301,9 +331,7 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz
     ZPASS_SETUP
     const int nzh = a.nzh;
     if (a.Dspec) {
-        zrepack(a.Dspec, line, nzz, nzh, has0, has1, xa);
-        __syncthreads();
-        dft_n<+1, FP>(smem, ld, fc, L);
+        zrepack_inverse<FP>(a.Dspec, smem, ld, fc, L, nzz, nzh, has0, has1, xa);
     }
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 D = a.Dspec ? line[k] : make_float2(0.f, 0.f);
@@ -382,9 +410,7 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz
 template <class FP>
 __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz_zinv_kernel(VzArgsI a) {
     ZPASS_SETUP
-    zrepack(a.spec, line, nzz, a.nzh, has0, has1, xa);
-    __syncthreads();
-    dft_n<+1, FP>(smem, ld, fc, L);
+    zrepack_inverse<FP>(a.spec, smem, ld, fc, L, nzz, a.nzh, has0, has1, xa);
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 v = line[k];
         if (has0) a.out[r0 + k] = v.x;
@@ -413,20 +439,31 @@ __global__ void __maxnreg__(QP_WIDE_REGS) lr_xconv_kernel(LrxArgs a) {
         const int kz = kz0 + c;
         smem[c * ld + ix] = (kz < nzh) ? a.in[(size_t)ix * nzh + kz] : make_float2(0.f, 0.f);
     }
-    for (int k = nxx + threadIdx.x; k < m; k += blockDim.x) line[k] = make_float2(0.f, 0.f);
-    __syncthreads();
-    fft_m<-1, FP>(smem, ld, fc, L);
-    for (int k = threadIdx.x; k < m; k += blockDim.x) X[threadIdx.y * ld + k] = line[k];
+    if constexpr (FP::kCompiled) {
+        // zero padding in the first pass, the spectrum straight into X
+        __syncthreads();
+        FP::template run_io<-1>(smem, ld, fc, L, ZeroPadIn{nxx}, CopyOut{X + threadIdx.y * ld});
+    } else {
+        for (int k = nxx + threadIdx.x; k < m; k += blockDim.x) line[k] = make_float2(0.f, 0.f);
+        __syncthreads();
+        fft_m<-1, FP>(smem, ld, fc, L);
+        for (int k = threadIdx.x; k < m; k += blockDim.x) X[threadIdx.y * ld + k] = line[k];
+    }
     const int kz = min(kz0 + (int)threadIdx.y, nzh - 1);
     const int mh = m / 2 + 1;
 #pragma unroll 1
     for (int b = 0; b < a.row; b++) {
         const float* tk = a.tab + ((size_t)b * nzh + kz) * mh;
         __syncthreads();
-        for (int k = threadIdx.x; k < m; k += blockDim.x)
-            line[k] = cscale(X[threadIdx.y * ld + k], __ldg(&tk[min(k, m - k)]));
-        __syncthreads();
-        fft_m<+1, FP>(smem, ld, fc, L);
+        if constexpr (FP::kCompiled) {
+            // the multiplier applied as the first inverse pass loads X
+            FP::template run_io<+1>(smem, ld, fc, L, EvenScaleIn{X + threadIdx.y * ld, tk, m}, LineOut{});
+        } else {
+            for (int k = threadIdx.x; k < m; k += blockDim.x)
+                line[k] = cscale(X[threadIdx.y * ld + k], __ldg(&tk[min(k, m - k)]));
+            __syncthreads();
+            fft_m<+1, FP>(smem, ld, fc, L);
+        }
         float2* out = a.out + (size_t)b * nxx * nzh;
         for (int g = t0; g < tot; g += nthr) {
             const int c = g & (L - 1), ix = g >> lg;
@@ -445,9 +482,7 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) lr
     const int nzh = a.nzh;
     float2* acc = smem + (size_t)(L + threadIdx.y) * ld;
     auto term = [&](int b, bool first) {
-        zrepack(a.Q + (size_t)b * nxx * nzh, line, nzz, nzh, has0, has1, xa);
-        __syncthreads();
-        dft_n<+1, FP>(smem, ld, fc, L);
+        zrepack_inverse<FP>(a.Q + (size_t)b * nxx * nzh, smem, ld, fc, L, nzz, nzh, has0, has1, xa);
         const float* cb = a.c + (size_t)b * nxx * nzz;
         for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
             const float2 v = line[k];
