@@ -308,7 +308,7 @@ struct LineIn {
     __device__ __forceinline__ float2 load(const float2* line, int i) const { return line[i]; }
 };
 struct LineOut {
-    static constexpr bool kSep = false;
+    static constexpr bool kSep = false, kEarly = false;
     __device__ __forceinline__ void store(float2* line, int i, float2 v) const { line[i] = v; }
 };
 // entries [n, m) of the line read as zeros (a zero-padded convolution)
@@ -319,24 +319,27 @@ struct ZeroPadIn {
         return (i < n) ? line[i] : make_float2(0.f, 0.f);
     }
 };
+// kEarly: a pure function of (i, v), applied to the outputs in registers before
+// the pass's barrier (its table loads then overlap the barrier wait); the
+// store after the barrier is plain.
 // outputs times a complex multiplier H[i] (the spectrum of a convolution kernel)
 struct MulOut {
-    static constexpr bool kSep = false;
+    static constexpr bool kSep = false, kEarly = true;
     const float2* __restrict__ H;
-    __device__ __forceinline__ void store(float2* line, int i, float2 v) const { line[i] = cmul(v, __ldg(&H[i])); }
+    __device__ __forceinline__ float2 apply(int i, float2 v) const { return cmul(v, __ldg(&H[i])); }
+    __device__ __forceinline__ void store(float2* line, int i, float2 v) const { line[i] = v; }
 };
 // outputs times an even real multiplier stored for 0..m/2 (tk[min(i, m - i)])
 struct EvenScaleOut {
-    static constexpr bool kSep = false;
+    static constexpr bool kSep = false, kEarly = true;
     const float* __restrict__ tk;
     int m;
-    __device__ __forceinline__ void store(float2* line, int i, float2 v) const {
-        line[i] = cscale(v, __ldg(&tk[min(i, m - i)]));
-    }
+    __device__ __forceinline__ float2 apply(int i, float2 v) const { return cscale(v, __ldg(&tk[min(i, m - i)])); }
+    __device__ __forceinline__ void store(float2* line, int i, float2 v) const { line[i] = v; }
 };
 // outputs to another buffer (dst: this thread's line there)
 struct CopyOut {
-    static constexpr bool kSep = true;
+    static constexpr bool kSep = true, kEarly = false;
     float2* dst;
     __device__ __forceinline__ void store(float2*, int i, float2 v) const { dst[i] = v; }
 };
@@ -359,15 +362,26 @@ struct EvenScaleIn {
 // in registers.  That is how lines longer than 768 butterflies of the smallest
 // radix (m above about 5000) stay in one CTA.  The first pass loads through
 // `in`, the last one stores through `out`.
+template <int R, int... Rest> constexpr int first_radix() { return R; }
+
 template <int S, int M, int NS, int TX, class In, class Out, int R, int... Rest>
 __device__ __forceinline__ void ct_passes(float2* line, const float2* __restrict__ tw, bool lact, const In& in,
-                                          const Out& out) {
+                                          const Out& out, float2 wpre) {
     constexpr bool kFirst = NS == 1, kLast = sizeof...(Rest) == 0;
     static_assert(!(kFirst && kLast && In::kSep && Out::kSep), "a one-pass transform between two other buffers");
     constexpr bool kSep = (kFirst && In::kSep) || (kLast && Out::kSep);
     constexpr int B = M / R;
     constexpr int NB = (TX == 0) ? 1 : (B + TX - 1) / TX;
     static_assert(NB * R <= 16, "butterflies of one thread must fit its registers");
+    // One butterfly per thread (TX = 0): the next pass's twiddle is loaded at
+    // the start of this pass, so its latency overlaps this pass's work and
+    // barriers (the pass receives its own as wpre).
+    float2 wnext = make_float2(1.f, 0.f);
+    if constexpr (TX == 0 && !kLast) {
+        constexpr int NS2 = NS * R, R2 = first_radix<Rest...>(), B2 = M / R2;
+        const int j = threadIdx.x;
+        if (lact && j < B2) wnext = __ldg(&tw[(j % NS2) * (M / (NS2 * R2))]);
+    }
     float2 v[NB][R];
     int k[NB];
 #pragma unroll
@@ -382,7 +396,7 @@ __device__ __forceinline__ void ct_passes(float2* line, const float2* __restrict
                 else v[q][r] = line[j + r * B];
             }
             if constexpr (NS > 1) {
-                float2 w1 = __ldg(&tw[k[q] * (M / (NS * R))]);
+                float2 w1 = (TX == 0) ? wpre : __ldg(&tw[k[q] * (M / (NS * R))]);
                 if (S > 0) w1.y = -w1.y;
                 float2 w = w1;
 #pragma unroll
@@ -392,6 +406,11 @@ __device__ __forceinline__ void ct_passes(float2* line, const float2* __restrict
                 }
             }
             dft<R, S>(v[q]);
+            if constexpr (kLast && Out::kEarly) {
+                const int base = (j - k[q]) * R + k[q];
+#pragma unroll
+                for (int r = 0; r < R; r++) v[q][r] = out.apply(base + r * NS, v[q][r]);
+            }
         }
     }
     if constexpr (!kSep) __syncthreads();
@@ -408,7 +427,7 @@ __device__ __forceinline__ void ct_passes(float2* line, const float2* __restrict
         }
     }
     __syncthreads();
-    if constexpr (!kLast) ct_passes<S, M, NS * R, TX, In, Out, Rest...>(line, tw, lact, in, out);
+    if constexpr (!kLast) ct_passes<S, M, NS * R, TX, In, Out, Rest...>(line, tw, lact, in, out, wnext);
 }
 
 template <int TX, int... Rs> struct CtFFTX {
@@ -424,7 +443,7 @@ template <int TX, int... Rs> struct CtFFTX {
     static constexpr bool kCompiled = true;
     template <int S> __device__ __forceinline__ static void run(float2* buf, int ld, const FFTCtx& c, int L) {
         ct_passes<S, M, 1, TX, LineIn, LineOut, Rs...>(buf + threadIdx.y * ld, c.w, threadIdx.y < L, LineIn{},
-                                                       LineOut{});
+                                                       LineOut{}, make_float2(1.f, 0.f));
     }
     // The same transform with first- and last-pass hooks (LineIn .. EvenScaleIn
     // above).  Caller has synchronised after filling what `in` reads; ends with
@@ -432,7 +451,8 @@ template <int TX, int... Rs> struct CtFFTX {
     template <int S, class In, class Out>
     __device__ __forceinline__ static void run_io(float2* buf, int ld, const FFTCtx& c, int L, const In& in,
                                                   const Out& out) {
-        ct_passes<S, M, 1, TX, In, Out, Rs...>(buf + threadIdx.y * ld, c.w, threadIdx.y < L, in, out);
+        ct_passes<S, M, 1, TX, In, Out, Rs...>(buf + threadIdx.y * ld, c.w, threadIdx.y < L, in, out,
+                                               make_float2(1.f, 0.f));
     }
     // host: is p exactly this plan (radices and, for TX > 0, threads per line)?
     static bool matches(const FFTPlanDev& p) {
