@@ -69,24 +69,45 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) ac
         __syncthreads();
         roundtrip_conv<FP>(smem, ld, fc, L, a.HzP);
         if (a.stage) cp_async_wait_all();
-        for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
-            const float2 d = line[k];
-            const float hb = a.h_bz[k], ha = a.h_az[k];
-            float2 nv = make_float2(0.f, 0.f);
-            if (has0) {
-                const float ps = hb * rd(1, ppz_in, 0, k) + ha * d.x;
-                a.psi_pz[r0 + k] = ps;
-                nv.x = rd(0, vz_in, 0, k) + a.dt * rd(2, bbz_in, 0, k) * (d.x + ps);
-                a.vz[r0 + k] = nv.x;
-            }
-            if (has1) {
-                const float ps = hb * rd(1, ppz_in, 1, k) + ha * d.y;
-                a.psi_pz[r1 + k] = ps;
-                nv.y = rd(0, vz_in, 1, k) + a.dt * rd(2, bbz_in, 1, k) * (d.y + ps);
-                a.vz[r1 + k] = nv.y;
-            }
-            line[k] = nv;
-        }
+        struct VIn {
+            float2 pp, v0, bb;
+            float hb, ha;
+        };
+        batched_for<kEpiBatchZ>(
+            threadIdx.x, nzz, blockDim.x,
+            [&](int k) {
+                VIn r{};
+                r.hb = a.h_bz[k];
+                r.ha = a.h_az[k];
+                if (has0) {
+                    r.pp.x = rd(1, ppz_in, 0, k);
+                    r.v0.x = rd(0, vz_in, 0, k);
+                    r.bb.x = rd(2, bbz_in, 0, k);
+                }
+                if (has1) {
+                    r.pp.y = rd(1, ppz_in, 1, k);
+                    r.v0.y = rd(0, vz_in, 1, k);
+                    r.bb.y = rd(2, bbz_in, 1, k);
+                }
+                return r;
+            },
+            [&](int k, const VIn& r) {
+                const float2 d = line[k];
+                float2 nv = make_float2(0.f, 0.f);
+                if (has0) {
+                    const float ps = r.hb * r.pp.x + r.ha * d.x;
+                    a.psi_pz[r0 + k] = ps;
+                    nv.x = r.v0.x + a.dt * r.bb.x * (d.x + ps);
+                    a.vz[r0 + k] = nv.x;
+                }
+                if (has1) {
+                    const float ps = r.hb * r.pp.y + r.ha * d.y;
+                    a.psi_pz[r1 + k] = ps;
+                    nv.y = r.v0.y + a.dt * r.bb.y * (d.y + ps);
+                    a.vz[r1 + k] = nv.y;
+                }
+                line[k] = nv;
+            });
     } else if (a.do_div) {
         zload_pair(a.vz, line, nzz, has0, has1, r0, r1);
     }
@@ -94,24 +115,43 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) ac
     __syncthreads();
     roundtrip_conv<FP>(smem, ld, fc, L, a.HzM);
     if (a.stage) cp_async_wait_all();
-    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
-        const float2 d = line[k];
-        const float ib = a.i_bz[k], ia = a.i_az[k];
-        float2 dv = make_float2(0.f, 0.f);
-        if (has0) {
-            const float ps = ib * rd(3, pvz_in, 0, k) + ia * d.x;
-            a.psi_vz[r0 + k] = ps;
-            dv.x = rd(4, dx_in, 0, k) + (d.x + ps);
-            a.div[r0 + k] = dv.x;
-        }
-        if (has1) {
-            const float ps = ib * rd(3, pvz_in, 1, k) + ia * d.y;
-            a.psi_vz[r1 + k] = ps;
-            dv.y = rd(4, dx_in, 1, k) + (d.y + ps);
-            a.div[r1 + k] = dv.y;
-        }
-        line[k] = dv;
-    }
+    struct DIn {
+        float2 pv, dx;
+        float ib, ia;
+    };
+    batched_for<kEpiBatchZ>(
+        threadIdx.x, nzz, blockDim.x,
+        [&](int k) {
+            DIn r{};
+            r.ib = a.i_bz[k];
+            r.ia = a.i_az[k];
+            if (has0) {
+                r.pv.x = rd(3, pvz_in, 0, k);
+                r.dx.x = rd(4, dx_in, 0, k);
+            }
+            if (has1) {
+                r.pv.y = rd(3, pvz_in, 1, k);
+                r.dx.y = rd(4, dx_in, 1, k);
+            }
+            return r;
+        },
+        [&](int k, const DIn& r) {
+            const float2 d = line[k];
+            float2 dv = make_float2(0.f, 0.f);
+            if (has0) {
+                const float ps = r.ib * r.pv.x + r.ia * d.x;
+                a.psi_vz[r0 + k] = ps;
+                dv.x = r.dx.x + (d.x + ps);
+                a.div[r0 + k] = dv.x;
+            }
+            if (has1) {
+                const float ps = r.ib * r.pv.y + r.ia * d.y;
+                a.psi_vz[r1 + k] = ps;
+                dv.y = r.dx.y + (d.y + ps);
+                a.div[r1 + k] = dv.y;
+            }
+            line[k] = dv;
+        });
     __syncthreads();
     roundtrip_conv<FP>(smem, ld, fc, L, a.kz2);
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
@@ -218,19 +258,54 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) ac
             __syncthreads();
         }
         const int pml = a.pml, nz = nzz - 2 * pml;
-        for (int g = T.t0; g < T.tot; g += T.nthr) {
-            int c, ix;
-            T.split(g, c, ix);
-            const int iz = T.iz0 + c;
-            if (iz >= nzz) continue;
-            const size_t i = (size_t)ix * nzz + iz;
-            const float pn = sf[T.sidx(c, ix, ld)];
-            a.p[i] = pn;
-            if (ix >= pml && ix < nxx - pml && iz >= pml && iz < nzz - pml) {
-                const size_t j = (size_t)(ix - pml) * nz + (iz - pml);
-                if (a.ssg) kahan_add(a.ssg, a.ssg_c, j, pn * pn);
-                if (a.img) kahan_add(a.img, a.img_c, j, a.ps[i] * pn);
+        if (!a.ssg && !a.img) {
+            for (int g = T.t0; g < T.tot; g += T.nthr) {
+                int c, ix;
+                T.split(g, c, ix);
+                const int iz = T.iz0 + c;
+                if (iz < nzz) a.p[(size_t)ix * nzz + iz] = sf[T.sidx(c, ix, ld)];
             }
+        } else {
+            // sums of the interior: s, s_c of the illumination and the image
+            // and the source wavefield, loaded a group of points at a time
+            struct Acc {
+                float s, sc, m, mc, ps;
+            };
+            batched_for<kEpiBatchX>(
+                T.t0, T.tot, T.nthr,
+                [&](int g) {
+                    Acc r{0.f, 0.f, 0.f, 0.f, 0.f};
+                    int c, ix;
+                    T.split(g, c, ix);
+                    const int iz = T.iz0 + c;
+                    if (iz < nzz && ix >= pml && ix < nxx - pml && iz >= pml && iz < nzz - pml) {
+                        const size_t j = (size_t)(ix - pml) * nz + (iz - pml);
+                        if (a.ssg) {
+                            r.s = a.ssg[j];
+                            r.sc = a.ssg_c[j];
+                        }
+                        if (a.img) {
+                            r.m = a.img[j];
+                            r.mc = a.img_c[j];
+                            r.ps = a.ps[(size_t)ix * nzz + iz];
+                        }
+                    }
+                    return r;
+                },
+                [&](int g, const Acc& r) {
+                    int c, ix;
+                    T.split(g, c, ix);
+                    const int iz = T.iz0 + c;
+                    if (iz >= nzz) return;
+                    const size_t i = (size_t)ix * nzz + iz;
+                    const float pn = sf[T.sidx(c, ix, ld)];
+                    a.p[i] = pn;
+                    if (ix >= pml && ix < nxx - pml && iz >= pml && iz < nzz - pml) {
+                        const size_t j = (size_t)(ix - pml) * nz + (iz - pml);
+                        if (a.ssg) kahan_add_v(a.ssg, a.ssg_c, j, r.s, r.sc, pn * pn);
+                        if (a.img) kahan_add_v(a.img, a.img_c, j, r.m, r.mc, r.ps * pn);
+                    }
+                });
         }
         have = true;
     }
@@ -247,24 +322,41 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) ac
         __syncthreads();
         roundtrip_conv<FP>(smem, ld, fc, L, a.HxP);
         if (a.stage) cp_async_wait_all();
-        for (int g = T.t0; g < T.tot; g += T.nthr) {
-            int c, ix;
-            T.split(g, c, ix);
-            const int iz = T.iz0 + c;
-            float nv = 0.f;
-            if (iz < nzz) {
-                const size_t i = (size_t)ix * nzz + iz;
-                const float d = sf[T.sidx(c, ix, ld)];
-                const float pp = a.stage ? S(5, g) : a.psi_px[i];
-                const float v0 = a.stage ? S(6, g) : a.vx[i];
-                const float bb = a.stage ? S(7, g) : a.bbx[i];
-                const float ps = a.h_bx[ix] * pp + a.h_ax[ix] * d;
-                a.psi_px[i] = ps;
-                nv = v0 + a.dt * bb * (d + ps);
-                a.vx[i] = nv;
-            }
-            sf[T.sidx(c, ix, ld)] = nv;
-        }
+        struct VIn {
+            float pp, v0, bb, hb, ha;
+        };
+        batched_for<kEpiBatchX>(
+            T.t0, T.tot, T.nthr,
+            [&](int g) {
+                VIn r{0.f, 0.f, 0.f, 0.f, 0.f};
+                int c, ix;
+                T.split(g, c, ix);
+                const int iz = T.iz0 + c;
+                if (iz < nzz) {
+                    const size_t i = (size_t)ix * nzz + iz;
+                    r.pp = a.stage ? S(5, g) : a.psi_px[i];
+                    r.v0 = a.stage ? S(6, g) : a.vx[i];
+                    r.bb = a.stage ? S(7, g) : a.bbx[i];
+                    r.hb = a.h_bx[ix];
+                    r.ha = a.h_ax[ix];
+                }
+                return r;
+            },
+            [&](int g, const VIn& r) {
+                int c, ix;
+                T.split(g, c, ix);
+                const int iz = T.iz0 + c;
+                float nv = 0.f;
+                if (iz < nzz) {
+                    const size_t i = (size_t)ix * nzz + iz;
+                    const float d = sf[T.sidx(c, ix, ld)];
+                    const float ps = r.hb * r.pp + r.ha * d;
+                    a.psi_px[i] = ps;
+                    nv = r.v0 + a.dt * r.bb * (d + ps);
+                    a.vx[i] = nv;
+                }
+                sf[T.sidx(c, ix, ld)] = nv;
+            });
         have = true;
     } else {
         have = false;
@@ -286,18 +378,34 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) ac
         __syncthreads();
         roundtrip_conv<FP>(smem, ld, fc, L, a.HxM);
         if (a.stage) cp_async_wait_all();
-        for (int g = T.t0; g < T.tot; g += T.nthr) {
-            int c, ix;
-            T.split(g, c, ix);
-            const int iz = T.iz0 + c;
-            if (iz >= nzz) continue;
-            const size_t i = (size_t)ix * nzz + iz;
-            const float d = sf[T.sidx(c, ix, ld)];
-            const float pv = a.stage ? S(8, g) : a.psi_vx[i];
-            const float ps = a.i_bx[ix] * pv + a.i_ax[ix] * d;
-            a.psi_vx[i] = ps;
-            a.Dx[i] = d + ps;
-        }
+        struct DIn {
+            float pv, ib, ia;
+        };
+        batched_for<kEpiBatchX>(
+            T.t0, T.tot, T.nthr,
+            [&](int g) {
+                DIn r{0.f, 0.f, 0.f};
+                int c, ix;
+                T.split(g, c, ix);
+                const int iz = T.iz0 + c;
+                if (iz < nzz) {
+                    r.pv = a.stage ? S(8, g) : a.psi_vx[(size_t)ix * nzz + iz];
+                    r.ib = a.i_bx[ix];
+                    r.ia = a.i_ax[ix];
+                }
+                return r;
+            },
+            [&](int g, const DIn& r) {
+                int c, ix;
+                T.split(g, c, ix);
+                const int iz = T.iz0 + c;
+                if (iz >= nzz) return;
+                const size_t i = (size_t)ix * nzz + iz;
+                const float d = sf[T.sidx(c, ix, ld)];
+                const float ps = r.ib * r.pv + r.ia * d;
+                a.psi_vx[i] = ps;
+                a.Dx[i] = d + ps;
+            });
     }
 }
 

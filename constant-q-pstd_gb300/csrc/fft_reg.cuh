@@ -322,6 +322,12 @@ struct ZeroPadIn {
 // kEarly: a pure function of (i, v), applied to the outputs in registers before
 // the pass's barrier (its table loads then overlap the barrier wait); the
 // store after the barrier is plain.
+// inputs times a complex multiplier H[i]
+struct MulIn {
+    static constexpr bool kSep = false;
+    const float2* __restrict__ H;
+    __device__ __forceinline__ float2 load(const float2* line, int i) const { return cmul(line[i], __ldg(&H[i])); }
+};
 // outputs times a complex multiplier H[i] (the spectrum of a convolution kernel)
 struct MulOut {
     static constexpr bool kSep = false, kEarly = true;

@@ -19,12 +19,46 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // Waits for every committed group but the most recent one.
 __device__ __forceinline__ void cp_async_wait_prior() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
+// Epilogue loops over k = k0, k0 + step, ... < n that read fields in global
+// memory and write fields in global memory.  The compiler may not move a later
+// iteration's loads above an earlier iteration's stores (the fields could
+// alias), so each iteration would wait out the latency of its own loads.  Here
+// the loads of U iterations (load(k) returns them) all issue before the first
+// of their bodies (use(k, loaded)) runs; the arithmetic is unchanged.
+template <int U, class LoadF, class UseF>
+__device__ __forceinline__ void batched_for(int k0, int n, int step, LoadF&& load, UseF&& use) {
+    using In = decltype(load(k0));
+    for (int kb = k0; kb < n; kb += U * step) {
+        In v[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int k = kb + u * step;
+            if (k < n) v[u] = load(k);
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int k = kb + u * step;
+            if (k < n) use(k, v[u]);
+        }
+    }
+}
+// U of the pass kernels' epilogues: x passes (one field value per point of a
+// row) and z passes (two rows per point, under tighter register caps)
+constexpr int kEpiBatchX = 4, kEpiBatchZ = 2;
+
 // Compensated accumulation s += v (Kahan), used for the image and the
 // illumination sums over thousands of steps.
 __device__ __forceinline__ void kahan_add(float* s, float* c, size_t i, float v) {
     const float y = v - c[i];
     const float t = s[i] + y;
     c[i] = (t - s[i]) - y;
+    s[i] = t;
+}
+// The same with s[i], c[i] already loaded (s0, c0).
+__device__ __forceinline__ void kahan_add_v(float* s, float* c, size_t i, float s0, float c0, float v) {
+    const float y = v - c0;
+    const float t = s0 + y;
+    c[i] = (t - s0) - y;
     s[i] = t;
 }
 

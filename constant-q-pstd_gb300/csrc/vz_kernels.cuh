@@ -78,24 +78,43 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz
     zload_pair(a.vz, line, nzz, has0, has1, r0, r1);
     __syncthreads();
     roundtrip_conv<FP>(smem, ld, fcc, L, a.HzM);
-    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
-        const float2 d = line[k];
-        const float ib = a.i_bz[k], ia = a.i_az[k];
-        float2 dv = make_float2(0.f, 0.f);
-        if (has0) {
-            const float ps = ib * a.psi_vz[r0 + k] + ia * d.x;
-            a.psi_vz[r0 + k] = ps;
-            dv.x = a.Dx[r0 + k] + (d.x + ps);
-            a.div[r0 + k] = dv.x;
-        }
-        if (has1) {
-            const float ps = ib * a.psi_vz[r1 + k] + ia * d.y;
-            a.psi_vz[r1 + k] = ps;
-            dv.y = a.Dx[r1 + k] + (d.y + ps);
-            a.div[r1 + k] = dv.y;
-        }
-        line[k] = dv;
-    }
+    struct DIn {
+        float2 pv, dx;
+        float ib, ia;
+    };
+    batched_for<kEpiBatchZ>(
+        threadIdx.x, nzz, blockDim.x,
+        [&](int k) {
+            DIn r{};
+            r.ib = a.i_bz[k];
+            r.ia = a.i_az[k];
+            if (has0) {
+                r.pv.x = a.psi_vz[r0 + k];
+                r.dx.x = a.Dx[r0 + k];
+            }
+            if (has1) {
+                r.pv.y = a.psi_vz[r1 + k];
+                r.dx.y = a.Dx[r1 + k];
+            }
+            return r;
+        },
+        [&](int k, const DIn& r) {
+            const float2 d = line[k];
+            float2 dv = make_float2(0.f, 0.f);
+            if (has0) {
+                const float ps = r.ib * r.pv.x + r.ia * d.x;
+                a.psi_vz[r0 + k] = ps;
+                dv.x = r.dx.x + (d.x + ps);
+                a.div[r0 + k] = dv.x;
+            }
+            if (has1) {
+                const float ps = r.ib * r.pv.y + r.ia * d.y;
+                a.psi_vz[r1 + k] = ps;
+                dv.y = r.dx.y + (d.y + ps);
+                a.div[r1 + k] = dv.y;
+            }
+            line[k] = dv;
+        });
     __syncthreads();
     dft_n<-1, FP>(smem, ld, fc, L);
     zunpack(line, a.G, nzz, nzh, has0, has1, xa);
@@ -307,19 +326,36 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz
     term(a.Y2, a.y2, 1.f, true);
     term(a.Y3, a.y3c, -1.f, false);
     term(a.Y4, a.y4c, -1.f, false);
-    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
-        const float2 t = acc[k];
-        float2 v = make_float2(0.f, 0.f);
-        if (has0) {
-            v.x = a.y1[r0 + k] * a.div[r0 + k] + t.x;
-            a.total[r0 + k] = v.x;
-        }
-        if (has1) {
-            v.y = a.y1[r1 + k] * a.div[r1 + k] + t.y;
-            a.total[r1 + k] = v.y;
-        }
-        line[k] = v;
-    }
+    struct TIn {
+        float2 y1, dv;
+    };
+    batched_for<kEpiBatchZ>(
+        threadIdx.x, nzz, blockDim.x,
+        [&](int k) {
+            TIn r{};
+            if (has0) {
+                r.y1.x = a.y1[r0 + k];
+                r.dv.x = a.div[r0 + k];
+            }
+            if (has1) {
+                r.y1.y = a.y1[r1 + k];
+                r.dv.y = a.div[r1 + k];
+            }
+            return r;
+        },
+        [&](int k, const TIn& r) {
+            const float2 t = acc[k];
+            float2 v = make_float2(0.f, 0.f);
+            if (has0) {
+                v.x = r.y1.x * r.dv.x + t.x;
+                a.total[r0 + k] = v.x;
+            }
+            if (has1) {
+                v.y = r.y1.y * r.dv.y + t.y;
+                a.total[r1 + k] = v.y;
+            }
+            line[k] = v;
+        });
     __syncthreads();
     dft_n<-1, FP>(smem, ld, fc, L);
     zunpack(line, a.T, nzz, nzh, has0, has1, xa);
@@ -364,20 +400,55 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz
         __syncthreads();
     }
     const int pml = a.pml, nz = nzz - 2 * pml;
-    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
-        const float2 pn = line[k];
-        for (int h = 0; h < 2; h++) {
-            const int ix = xa + h;
-            if (ix >= nxx) break;
-            const float v = h ? pn.y : pn.x;
-            const size_t i = (size_t)ix * nzz + k;
-            a.p[i] = v;
-            if (ix >= pml && ix < nxx - pml && k >= pml && k < nzz - pml) {
-                const size_t j = (size_t)(ix - pml) * nz + (k - pml);
-                if (a.ssg) kahan_add(a.ssg, a.ssg_c, j, v * v);
-                if (a.img) kahan_add(a.img, a.img_c, j, a.ps[i] * v);
-            }
+    if (!a.ssg && !a.img) {
+        for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
+            const float2 pn = line[k];
+            if (has0) a.p[r0 + k] = pn.x;
+            if (has1) a.p[r1 + k] = pn.y;
         }
+    } else {
+        // sums of the interior (illumination, image) and the source
+        // wavefield of both rows, loaded a group of points at a time
+        struct Acc {
+            float s[2], sc[2], m[2], mc[2], ps[2];
+        };
+        batched_for<kEpiBatchZ>(
+            threadIdx.x, nzz, blockDim.x,
+            [&](int k) {
+                Acc r{};
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int ix = xa + h;
+                    if (ix < nxx && ix >= pml && ix < nxx - pml && k >= pml && k < nzz - pml) {
+                        const size_t j = (size_t)(ix - pml) * nz + (k - pml);
+                        if (a.ssg) {
+                            r.s[h] = a.ssg[j];
+                            r.sc[h] = a.ssg_c[j];
+                        }
+                        if (a.img) {
+                            r.m[h] = a.img[j];
+                            r.mc[h] = a.img_c[j];
+                            r.ps[h] = a.ps[(size_t)ix * nzz + k];
+                        }
+                    }
+                }
+                return r;
+            },
+            [&](int k, const Acc& r) {
+                const float2 pn = line[k];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int ix = xa + h;
+                    if (ix >= nxx) break;
+                    const float v = h ? pn.y : pn.x;
+                    a.p[(size_t)ix * nzz + k] = v;
+                    if (ix >= pml && ix < nxx - pml && k >= pml && k < nzz - pml) {
+                        const size_t j = (size_t)(ix - pml) * nz + (k - pml);
+                        if (a.ssg) kahan_add_v(a.ssg, a.ssg_c, j, r.s[h], r.sc[h], v * v);
+                        if (a.img) kahan_add_v(a.img, a.img_c, j, r.m[h], r.mc[h], r.ps[h] * v);
+                    }
+                }
+            });
     }
     __syncthreads();
     // forward z transform of the new p: half spectrum for the aux operator and
@@ -385,25 +456,55 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz
     dft_n<-1, FP>(smem, ld, fc, L);
     zunpack(line, a.P, nzz, nzh, has0, has1, xa);
     __syncthreads();
-    for (int k = threadIdx.x; k < nzz; k += blockDim.x) line[k] = cmul(line[k], __ldg(&a.HzP[k]));
-    __syncthreads();
-    dft_n<+1, FP>(smem, ld, fc, L);
-    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
-        const float2 d = line[k];
-        const float hb = a.h_bz[k], ha = a.h_az[k];
-        if (has0) {
-            const size_t i = r0 + k;
-            const float ps = hb * a.psi_pz[i] + ha * d.x;
-            a.psi_pz[i] = ps;
-            a.vz[i] = a.vz[i] + a.dt * a.bbz[i] * (d.x + ps);
+    if constexpr (FP::kCompiled) {
+        if (!fc.blue) {
+            // the multiplier applied as the first inverse pass loads the line
+            FP::template run_io<+1>(smem, ld, fc, L, MulIn{a.HzP}, LineOut{});
+        } else {
+            for (int k = threadIdx.x; k < nzz; k += blockDim.x) line[k] = cmul(line[k], __ldg(&a.HzP[k]));
+            __syncthreads();
+            dft_n<+1, FP>(smem, ld, fc, L);
         }
-        if (has1) {
-            const size_t i = r1 + k;
-            const float ps = hb * a.psi_pz[i] + ha * d.y;
-            a.psi_pz[i] = ps;
-            a.vz[i] = a.vz[i] + a.dt * a.bbz[i] * (d.y + ps);
-        }
+    } else {
+        for (int k = threadIdx.x; k < nzz; k += blockDim.x) line[k] = cmul(line[k], __ldg(&a.HzP[k]));
+        __syncthreads();
+        dft_n<+1, FP>(smem, ld, fc, L);
     }
+    struct VIn {
+        float2 pp, v0, bb;
+        float hb, ha;
+    };
+    batched_for<kEpiBatchZ>(
+        threadIdx.x, nzz, blockDim.x,
+        [&](int k) {
+            VIn r{};
+            r.hb = a.h_bz[k];
+            r.ha = a.h_az[k];
+            if (has0) {
+                r.pp.x = a.psi_pz[r0 + k];
+                r.v0.x = a.vz[r0 + k];
+                r.bb.x = a.bbz[r0 + k];
+            }
+            if (has1) {
+                r.pp.y = a.psi_pz[r1 + k];
+                r.v0.y = a.vz[r1 + k];
+                r.bb.y = a.bbz[r1 + k];
+            }
+            return r;
+        },
+        [&](int k, const VIn& r) {
+            const float2 d = line[k];
+            if (has0) {
+                const float ps = r.hb * r.pp.x + r.ha * d.x;
+                a.psi_pz[r0 + k] = ps;
+                a.vz[r0 + k] = r.v0.x + a.dt * r.bb.x * (d.x + ps);
+            }
+            if (has1) {
+                const float ps = r.hb * r.pp.y + r.ha * d.y;
+                a.psi_pz[r1 + k] = ps;
+                a.vz[r1 + k] = r.v0.y + a.dt * r.bb.y * (d.y + ps);
+            }
+        });
 }
 
 // ---- z inverse only -------------------------------------------------------------
