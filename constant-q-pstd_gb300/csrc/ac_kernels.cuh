@@ -216,35 +216,55 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) ac
     bool have = false;  // smem holds the packed field for the next transform
     if (P) {
         // div feeds the first transform now and the p update later
-        for (int g = T.t0; g < T.tot; g += T.nthr) {
-            int c, ix;
-            T.split(g, c, ix);
-            const int iz = T.iz0 + c;
-            const float v = (iz < nzz) ? a.div[(size_t)ix * nzz + iz] : 0.f;
-            sf[T.sidx(c, ix, ld)] = v;
-            if (a.stage) S(0, g) = v;
-        }
+        batched_for<kEpiBatchX>(
+            T.t0, T.tot, T.nthr,
+            [&](int g) {
+                int c, ix;
+                T.split(g, c, ix);
+                const int iz = T.iz0 + c;
+                return (iz < nzz) ? a.div[(size_t)ix * nzz + iz] : 0.f;
+            },
+            [&](int g, float v) {
+                int c, ix;
+                T.split(g, c, ix);
+                sf[T.sidx(c, ix, ld)] = v;
+                if (a.stage) S(0, g) = v;
+            });
         __syncthreads();
         roundtrip_conv<FP>(smem, ld, fc, L, a.kx2);
         if (a.stage) cp_async_wait_all();
-        for (int g = T.t0; g < T.tot; g += T.nthr) {
-            int c, ix;
-            T.split(g, c, ix);
-            const int iz = T.iz0 + c;
-            float pn = 0.f;
-            if (iz < nzz) {
-                const size_t i = (size_t)ix * nzz + iz;
-                const float lz = a.stage ? S(1, g) : a.Lz[i];
-                const float p0 = a.stage ? S(2, g) : a.p[i];
-                const float c1 = a.stage ? S(3, g) : a.c1[i];
-                const float c2 = a.stage ? S(4, g) : a.c2[i];
-                const float dv = a.stage ? S(0, g) : a.div[i];
-                const float lap = sf[T.sidx(c, ix, ld)] + lz;
-                pn = p0 + c1 * (dv - c2 * lap);
-                if (ix == a.xs && iz == a.zs) pn += a.src;
-            }
-            sf[T.sidx(c, ix, ld)] = pn;
-        }
+        struct PIn {
+            float lz, p0, c1, c2, dv;
+        };
+        batched_for<kEpiBatchX>(
+            T.t0, T.tot, T.nthr,
+            [&](int g) {
+                PIn r{0.f, 0.f, 0.f, 0.f, 0.f};
+                int c, ix;
+                T.split(g, c, ix);
+                const int iz = T.iz0 + c;
+                if (iz < nzz) {
+                    const size_t i = (size_t)ix * nzz + iz;
+                    r.lz = a.stage ? S(1, g) : a.Lz[i];
+                    r.p0 = a.stage ? S(2, g) : a.p[i];
+                    r.c1 = a.stage ? S(3, g) : a.c1[i];
+                    r.c2 = a.stage ? S(4, g) : a.c2[i];
+                    r.dv = a.stage ? S(0, g) : a.div[i];
+                }
+                return r;
+            },
+            [&](int g, const PIn& r) {
+                int c, ix;
+                T.split(g, c, ix);
+                const int iz = T.iz0 + c;
+                float pn = 0.f;
+                if (iz < nzz) {
+                    const float lap = sf[T.sidx(c, ix, ld)] + r.lz;
+                    pn = r.p0 + r.c1 * (r.dv - r.c2 * lap);
+                    if (ix == a.xs && iz == a.zs) pn += a.src;
+                }
+                sf[T.sidx(c, ix, ld)] = pn;
+            });
         __syncthreads();
         // receivers of this tile: record (source side) or inject (receiver side)
         if (a.rec_off) {
@@ -312,12 +332,7 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) ac
     if (a.do_v) {
         if (!have) {
             if (a.stage) cp_async_wait_prior();  // p (first group) has landed
-            for (int g = T.t0; g < T.tot; g += T.nthr) {
-                int c, ix;
-                T.split(g, c, ix);
-                const int iz = T.iz0 + c;
-                sf[T.sidx(c, ix, ld)] = (iz < nzz) ? (a.stage ? S(2, g) : a.p[(size_t)ix * nzz + iz]) : 0.f;
-            }
+            xfill(sf, T, ld, [&](int g, int ix, int iz) { return a.stage ? S(2, g) : a.p[(size_t)ix * nzz + iz]; });
         }
         __syncthreads();
         roundtrip_conv<FP>(smem, ld, fc, L, a.HxP);
@@ -368,12 +383,7 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) ac
                 if (P) cp_async_wait_all();
                 else cp_async_wait_prior();
             }
-            for (int g = T.t0; g < T.tot; g += T.nthr) {
-                int c, ix;
-                T.split(g, c, ix);
-                const int iz = T.iz0 + c;
-                sf[T.sidx(c, ix, ld)] = (iz < nzz) ? (a.stage ? S(6, g) : a.vx[(size_t)ix * nzz + iz]) : 0.f;
-            }
+            xfill(sf, T, ld, [&](int g, int ix, int iz) { return a.stage ? S(6, g) : a.vx[(size_t)ix * nzz + iz]; });
         }
         __syncthreads();
         roundtrip_conv<FP>(smem, ld, fc, L, a.HxM);

@@ -65,12 +65,10 @@ __device__ __forceinline__ void kahan_add_v(float* s, float* c, size_t i, float 
 // z passes: this thread's line packs x rows r0 (re) and r1 (im).
 __device__ __forceinline__ void zload_pair(const float* __restrict__ f, float2* line, int nzz, bool has0, bool has1,
                                            size_t r0, size_t r1) {
-    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
-        float2 v;
-        v.x = has0 ? f[r0 + k] : 0.f;
-        v.y = has1 ? f[r1 + k] : 0.f;
-        line[k] = v;
-    }
+    batched_for<kEpiBatchX>(
+        threadIdx.x, nzz, blockDim.x,
+        [&](int k) { return make_float2(has0 ? f[r0 + k] : 0.f, has1 ? f[r1 + k] : 0.f); },
+        [&](int k, float2 v) { line[k] = v; });
 }
 
 // Half spectra in kz: S[ix*nzh + kz], kz in [0, nzz/2].  Two real z-lines a, b
@@ -135,13 +133,23 @@ struct XTile {
     __device__ __forceinline__ int sidx(int c, int ix, int ld) const { return 2 * ((c >> 1) * ld + ix) + (c & 1); }
 };
 
-__device__ __forceinline__ void xload(const float* __restrict__ f, float* sf, const XTile& T, int ld) {
-    for (int g = T.t0; g < T.tot; g += T.nthr) {
-        int c, ix;
-        T.split(g, c, ix);
-        const int iz = T.iz0 + c;
-        sf[T.sidx(c, ix, ld)] = (iz < T.nzz) ? f[(size_t)ix * T.nzz + iz] : 0.f;
-    }
+// the packed shared lines <- get(g, ix, iz) for the tile's columns (0 past nzz),
+// a group of points' loads in flight at a time
+template <class Get>
+__device__ __forceinline__ void xfill(float* sf, const XTile& T, int ld, Get&& get) {
+    batched_for<kEpiBatchX>(
+        T.t0, T.tot, T.nthr,
+        [&](int g) {
+            int c, ix;
+            T.split(g, c, ix);
+            const int iz = T.iz0 + c;
+            return (iz < T.nzz) ? get(g, ix, iz) : 0.f;
+        },
+        [&](int g, float v) {
+            int c, ix;
+            T.split(g, c, ix);
+            sf[T.sidx(c, ix, ld)] = v;
+        });
 }
 
 }  // namespace qp

@@ -41,6 +41,20 @@ __device__ __forceinline__ void zrepack_inverse(const float2* __restrict__ S, fl
     dft_n<+1, FP>(smem, ld, fc, L);
 }
 
+// The L kz columns kz0 .. of the half spectra `in` into the shared lines (line
+// c = column kz0 + c, zeros past nzh), a group of points' loads in flight at a time.
+__device__ __forceinline__ void kzfill(float2* smem, const float2* __restrict__ in, int ld, int L, int lg, int kz0,
+                                       int nxx, int nzh, int t0, int nthr) {
+    batched_for<kEpiBatchX>(
+        t0, L * nxx, nthr,
+        [&](int g) {
+            const int c = g & (L - 1), ix = g >> lg;
+            const int kz = kz0 + c;
+            return (kz < nzh) ? in[(size_t)ix * nzh + kz] : make_float2(0.f, 0.f);
+        },
+        [&](int g, float2 v) { smem[(g & (L - 1)) * ld + (g >> lg)] = v; });
+}
+
 #define ZPASS_SETUP                                                  \
     extern __shared__ float2 smem[];                                 \
     __shared__ FFTPass s_pass[QP_MAXST];                             \
@@ -149,11 +163,7 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_PASS_REGS : QP_EXACT_REGS) 
     const int nout = (a.mode == 0) ? 3 : 1;
     float2* X = smem + (size_t)L * ld;  // kept forward spectrum (three-output mode)
     float2* line = smem + threadIdx.y * ld;
-    for (int g = t0; g < tot; g += nthr) {
-        const int c = g & (L - 1), ix = g >> lg;
-        const int kz = kz0 + c;
-        smem[c * ld + ix] = (kz < nzh) ? a.in[(size_t)ix * nzh + kz] : make_float2(0.f, 0.f);
-    }
+    kzfill(smem, a.in, ld, L, lg, kz0, nxx, nzh, t0, nthr);
     __syncthreads();
     dft_n<-1, FP>(smem, ld, fc, L);
     if (nout == 3) {
@@ -211,11 +221,7 @@ __global__ void __maxnreg__(NOUT == 3 ? QP_WIDE_REGS : FP::kMaxRadix <= 12 ? QP_
     constexpr int nout = NOUT;
     float2* X = smem + (size_t)L * ld;  // kept forward spectrum (three-output mode)
     float2* line = smem + threadIdx.y * ld;
-    for (int g = t0; g < tot; g += nthr) {
-        const int c = g & (L - 1), ix = g >> lg;
-        const int kz = kz0 + c;
-        smem[c * ld + ix] = (kz < nzh) ? a.in[(size_t)ix * nzh + kz] : make_float2(0.f, 0.f);
-    }
+    kzfill(smem, a.in, ld, L, lg, kz0, nxx, nzh, t0, nthr);
     if constexpr (!FP::kCompiled)
         for (int k = nxx + threadIdx.x; k < m; k += blockDim.x) line[k] = make_float2(0.f, 0.f);
     __syncthreads();
@@ -369,21 +375,46 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) vz
     if (a.Dspec) {
         zrepack_inverse<FP>(a.Dspec, smem, ld, fc, L, nzz, nzh, has0, has1, xa);
     }
-    for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
-        const float2 D = a.Dspec ? line[k] : make_float2(0.f, 0.f);
-        float2 pn = make_float2(0.f, 0.f);
-        if (has0) {
-            const size_t i = r0 + k;
-            pn.x = a.p[i] + a.e1[i] * (a.total[i] + a.sgn * a.e2[i] * D.x) + a.sgn * a.e3[i] * a.aux[i];
-            if (xa == a.xs && k == a.zs) pn.x += a.src;
-        }
-        if (has1) {
-            const size_t i = r1 + k;
-            pn.y = a.p[i] + a.e1[i] * (a.total[i] + a.sgn * a.e2[i] * D.y) + a.sgn * a.e3[i] * a.aux[i];
-            if (xa + 1 == a.xs && k == a.zs) pn.y += a.src;
-        }
-        line[k] = pn;
-    }
+    struct PIn {
+        float2 p, e1, tot, e2, e3, aux;
+    };
+    batched_for<kEpiBatchZ>(
+        threadIdx.x, nzz, blockDim.x,
+        [&](int k) {
+            PIn r{};
+            if (has0) {
+                const size_t i = r0 + k;
+                r.p.x = a.p[i];
+                r.e1.x = a.e1[i];
+                r.tot.x = a.total[i];
+                r.e2.x = a.e2[i];
+                r.e3.x = a.e3[i];
+                r.aux.x = a.aux[i];
+            }
+            if (has1) {
+                const size_t i = r1 + k;
+                r.p.y = a.p[i];
+                r.e1.y = a.e1[i];
+                r.tot.y = a.total[i];
+                r.e2.y = a.e2[i];
+                r.e3.y = a.e3[i];
+                r.aux.y = a.aux[i];
+            }
+            return r;
+        },
+        [&](int k, const PIn& r) {
+            const float2 D = a.Dspec ? line[k] : make_float2(0.f, 0.f);
+            float2 pn = make_float2(0.f, 0.f);
+            if (has0) {
+                pn.x = r.p.x + r.e1.x * (r.tot.x + a.sgn * r.e2.x * D.x) + a.sgn * r.e3.x * r.aux.x;
+                if (xa == a.xs && k == a.zs) pn.x += a.src;
+            }
+            if (has1) {
+                pn.y = r.p.y + r.e1.y * (r.tot.y + a.sgn * r.e2.y * D.y) + a.sgn * r.e3.y * r.aux.y;
+                if (xa + 1 == a.xs && k == a.zs) pn.y += a.src;
+            }
+            line[k] = pn;
+        });
     __syncthreads();
     const int ix0 = blockIdx.x * 2 * L;
     if (a.rec_off) {
@@ -535,11 +566,7 @@ __global__ void __maxnreg__(QP_WIDE_REGS) lr_xconv_kernel(LrxArgs a) {
     const int tot = L * nxx;
     float2* X = smem + (size_t)L * ld;  // kept forward spectrum
     float2* line = smem + threadIdx.y * ld;
-    for (int g = t0; g < tot; g += nthr) {
-        const int c = g & (L - 1), ix = g >> lg;
-        const int kz = kz0 + c;
-        smem[c * ld + ix] = (kz < nzh) ? a.in[(size_t)ix * nzh + kz] : make_float2(0.f, 0.f);
-    }
+    kzfill(smem, a.in, ld, L, lg, kz0, nxx, nzh, t0, nthr);
     if constexpr (FP::kCompiled) {
         // zero padding in the first pass, the spectrum straight into X
         __syncthreads();
