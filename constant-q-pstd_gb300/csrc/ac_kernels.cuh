@@ -332,7 +332,8 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) ac
     if (a.do_v) {
         if (!have) {
             if (a.stage) cp_async_wait_prior();  // p (first group) has landed
-            xfill(sf, T, ld, [&](int g, int ix, int iz) { return a.stage ? S(2, g) : a.p[(size_t)ix * nzz + iz]; });
+            xfill<x_epi_batch<FP>()>(sf, T, ld,
+                                     [&](int g, int ix, int iz) { return a.stage ? S(2, g) : a.p[(size_t)ix * nzz + iz]; });
         }
         __syncthreads();
         roundtrip_conv<FP>(smem, ld, fc, L, a.HxP);
@@ -340,7 +341,7 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) ac
         struct VIn {
             float pp, v0, bb, hb, ha;
         };
-        batched_for<kEpiBatchX>(
+        batched_for<x_epi_batch<FP>()>(
             T.t0, T.tot, T.nthr,
             [&](int g) {
                 VIn r{0.f, 0.f, 0.f, 0.f, 0.f};
@@ -383,7 +384,8 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) ac
                 if (P) cp_async_wait_all();
                 else cp_async_wait_prior();
             }
-            xfill(sf, T, ld, [&](int g, int ix, int iz) { return a.stage ? S(6, g) : a.vx[(size_t)ix * nzz + iz]; });
+            xfill<x_epi_batch<FP>()>(sf, T, ld,
+                                     [&](int g, int ix, int iz) { return a.stage ? S(6, g) : a.vx[(size_t)ix * nzz + iz]; });
         }
         __syncthreads();
         roundtrip_conv<FP>(smem, ld, fc, L, a.HxM);
@@ -391,7 +393,7 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) ac
         struct DIn {
             float pv, ib, ia;
         };
-        batched_for<kEpiBatchX>(
+        batched_for<x_epi_batch<FP>()>(
             T.t0, T.tot, T.nthr,
             [&](int g) {
                 DIn r{0.f, 0.f, 0.f};

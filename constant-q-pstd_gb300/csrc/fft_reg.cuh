@@ -289,6 +289,7 @@ __device__ __forceinline__ FFTCtx make_ctx(const FFTPlanDev& pl, FFTPass* s_pass
 template <int RMAX> struct RtFFT {
     static constexpr int kMaxRadix = RMAX;
     static constexpr bool kCompiled = false;
+    static constexpr int kLen = 0;  // the length is a run-time value
     template <int S> __device__ __forceinline__ static void run(float2* buf, int ld, const FFTCtx& c, int L) {
         fft_m_impl<S, RMAX>(buf, ld, c.sp, c.nst, c.w, L);
     }
@@ -447,6 +448,7 @@ template <int TX, int... Rs> struct CtFFTX {
         return r;
     }();
     static constexpr bool kCompiled = true;
+    static constexpr int kLen = M;
     template <int S> __device__ __forceinline__ static void run(float2* buf, int ld, const FFTCtx& c, int L) {
         ct_passes<S, M, 1, TX, LineIn, LineOut, Rs...>(buf + threadIdx.y * ld, c.w, threadIdx.y < L, LineIn{},
                                                        LineOut{}, make_float2(1.f, 0.f));

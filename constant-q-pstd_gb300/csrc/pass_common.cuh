@@ -43,8 +43,13 @@ __device__ __forceinline__ void batched_for(int k0, int n, int step, LoadF&& loa
     }
 }
 // U of the pass kernels' epilogues: x passes (one field value per point of a
-// row) and z passes (two rows per point, under tighter register caps)
+// row) and z passes (two rows per point, under tighter register caps).  x
+// lines of a compiled length of 2048 or more leave each thread 10 or more
+// points of its tile and take 8 at a time (6 in the radix-12 instances, whose
+// 48-register cap spills at 8); measured on the 5040-point lines of the large
+// RTM grid: 8.8 -> 9.2 Gpts/s, the Q-RTM batch 8.37 -> 8.44.
 constexpr int kEpiBatchX = 4, kEpiBatchZ = 2;
+template <class FP> constexpr int x_epi_batch() { return FP::kLen < 2048 ? kEpiBatchX : FP::kMaxRadix <= 12 ? 6 : 8; }
 
 // Compensated accumulation s += v (Kahan), used for the image and the
 // illumination sums over thousands of steps.
@@ -135,9 +140,9 @@ struct XTile {
 
 // the packed shared lines <- get(g, ix, iz) for the tile's columns (0 past nzz),
 // a group of points' loads in flight at a time
-template <class Get>
+template <int U, class Get>
 __device__ __forceinline__ void xfill(float* sf, const XTile& T, int ld, Get&& get) {
-    batched_for<kEpiBatchX>(
+    batched_for<U>(
         T.t0, T.tot, T.nthr,
         [&](int g) {
             int c, ix;

@@ -43,9 +43,10 @@ __device__ __forceinline__ void zrepack_inverse(const float2* __restrict__ S, fl
 
 // The L kz columns kz0 .. of the half spectra `in` into the shared lines (line
 // c = column kz0 + c, zeros past nzh), a group of points' loads in flight at a time.
+template <int U>
 __device__ __forceinline__ void kzfill(float2* smem, const float2* __restrict__ in, int ld, int L, int lg, int kz0,
                                        int nxx, int nzh, int t0, int nthr) {
-    batched_for<kEpiBatchX>(
+    batched_for<U>(
         t0, L * nxx, nthr,
         [&](int g) {
             const int c = g & (L - 1), ix = g >> lg;
@@ -163,7 +164,7 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_PASS_REGS : QP_EXACT_REGS) 
     const int nout = (a.mode == 0) ? 3 : 1;
     float2* X = smem + (size_t)L * ld;  // kept forward spectrum (three-output mode)
     float2* line = smem + threadIdx.y * ld;
-    kzfill(smem, a.in, ld, L, lg, kz0, nxx, nzh, t0, nthr);
+    kzfill<x_epi_batch<FP>()>(smem, a.in, ld, L, lg, kz0, nxx, nzh, t0, nthr);
     __syncthreads();
     dft_n<-1, FP>(smem, ld, fc, L);
     if (nout == 3) {
@@ -221,7 +222,7 @@ __global__ void __maxnreg__(NOUT == 3 ? QP_WIDE_REGS : FP::kMaxRadix <= 12 ? QP_
     constexpr int nout = NOUT;
     float2* X = smem + (size_t)L * ld;  // kept forward spectrum (three-output mode)
     float2* line = smem + threadIdx.y * ld;
-    kzfill(smem, a.in, ld, L, lg, kz0, nxx, nzh, t0, nthr);
+    kzfill<x_epi_batch<FP>()>(smem, a.in, ld, L, lg, kz0, nxx, nzh, t0, nthr);
     if constexpr (!FP::kCompiled)
         for (int k = nxx + threadIdx.x; k < m; k += blockDim.x) line[k] = make_float2(0.f, 0.f);
     __syncthreads();
@@ -566,7 +567,7 @@ __global__ void __maxnreg__(QP_WIDE_REGS) lr_xconv_kernel(LrxArgs a) {
     const int tot = L * nxx;
     float2* X = smem + (size_t)L * ld;  // kept forward spectrum
     float2* line = smem + threadIdx.y * ld;
-    kzfill(smem, a.in, ld, L, lg, kz0, nxx, nzh, t0, nthr);
+    kzfill<x_epi_batch<FP>()>(smem, a.in, ld, L, lg, kz0, nxx, nzh, t0, nthr);
     if constexpr (FP::kCompiled) {
         // zero padding in the first pass, the spectrum straight into X
         __syncthreads();
