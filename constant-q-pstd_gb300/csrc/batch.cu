@@ -59,11 +59,39 @@ extern "C" int qpstd_batch_sync(qpstd_batch* b) {
     return QPSTD_OK;
 }
 
+// Stream priorities by work: every shot gets the same number of kernel
+// launches per round, but a wide window's kernels run longer, so with equal
+// priorities the narrow shots finish first and the last part of the batch
+// runs a few wide shots on a partly idle GPU.  The widest shots get the
+// highest priority (the CTA scheduler then serves them first), in as many
+// classes as the device has priorities.
+static int prioritise_by_work(qpstd_batch* b) {
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return QPSTD_OK;
+    const int levels = least - greatest + 1;
+    const int n = (int)b->shots.size();
+    if (levels < 2 || n < 2) return QPSTD_OK;
+    std::vector<int> order(n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    auto work = [&](int i) {
+        const qpstd_shot_desc& d = b->shots[i]->d;
+        return (double)d.nxx * d.nzz * d.nt;
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work(x) < work(y); });
+    for (int r = 0; r < n; r++) {
+        const int cls = (int)((long long)r * levels / n);  // 0: least work
+        const int rc = shot_set_priority(b->shots[order[r]], least - cls);
+        if (rc) return rc;
+    }
+    return QPSTD_OK;
+}
+
 // All shots' RTM, their revolve actions interleaved round-robin; advances are
 // enqueued `slice` steps at a time.  Returns after enqueueing everything (the
 // results are ready after qpstd_batch_sync / qpstd_shot_get_image).
 extern "C" int qpstd_batch_rtm_device(qpstd_batch* b, int slice) {
     if (!b) return QPSTD_EINVAL;
+    if (const int rc = prioritise_by_work(b)) return rc;
     for (qpstd_shot* s : b->shots) {
         const int rc = rtm_begin(s);
         if (rc) return rc;

@@ -1259,6 +1259,20 @@ extern "C" int qpstd_shot_profile_read(qpstd_shot* s, int nkinds, double* ms, lo
     return QPSTD_OK;
 }
 extern "C" long long qpstd_shot_forward_steps(const qpstd_shot* s) { return s ? s->fwd_steps : -1; }
+int shot_set_priority(qpstd_shot* s, int prio) {
+    if (!s) return fail(QPSTD_EINVAL, "null shot");
+    CK(cudaStreamSynchronize(s->stream));
+    cudaStream_t st = nullptr;
+    CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio));
+    if (s->plain.have_plan && cufftSetStream(s->plain.plan, st) != CUFFT_SUCCESS) {
+        cudaStreamDestroy(st);
+        return fail(QPSTD_ECUDA, "cufftSetStream failed");
+    }
+    cudaStreamDestroy(s->stream);
+    s->stream = st;
+    return QPSTD_OK;
+}
+
 extern "C" int qpstd_shot_sync(qpstd_shot* s) {
     if (!s) return fail(QPSTD_EINVAL, "null shot");
     CK(cudaStreamSynchronize(s->stream));

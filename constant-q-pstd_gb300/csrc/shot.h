@@ -50,6 +50,8 @@ int rtm_action(qpstd_shot* s);  // 0: more actions, 1: finished, < 0: error code
 // qpstd_shot_create with options: tune runs the lines-per-CTA autotuner, arena
 // (may be null) supplies the device buffers.
 int shot_create_ex(const qpstd_shot_desc* d, qpstd_shot** out, bool tune, qp::Arena* arena);
+// Moves the shot to a new stream of CUDA priority prio (after its work so far).
+int shot_set_priority(qpstd_shot* s, int prio);
 // Modeling steps t0 .. t0+n-1 with the gather kept on the device (see shot.cu).
 int model_slice(qpstd_shot* s, int t0, int n);
 // A device buffer owned by the shot (its arena's when it has one); freed at destroy.
