@@ -58,12 +58,11 @@ void launch_lr_xconv(const LrxArgs& a, cudaStream_t s) {
 void launch_lr_zsum(const LrsArgs& a, cudaStream_t s) {
     const dim3 blk(a.pl.tx, a.L);
     const size_t sm = lsm(a.L, a.pl.m, 2);
-    for (int b0 = 0; b0 < a.row; b0 += 3) {
-        const int nb = min(3, a.row - b0);
-#define L_(FPT) lr_zsum_kernel<FPT><<<zgrid(a.nxx, a.L), blk, sm, s>>>(a, b0, nb)
-        QP_DISPATCH(ZPlans, a.pl, NoExtraPlan{}, plan_max_radix(a.pl) <= 12, L_);
+#define L_(FPT)                                                                         \
+    for (int b0 = 0; b0 < a.row; b0 += lr_terms<FPT>())                                 \
+    lr_zsum_kernel<FPT><<<zgrid(a.nxx, a.L), blk, sm, s>>>(a, b0, min(lr_terms<FPT>(), a.row - b0))
+    QP_DISPATCH(ZPlans, a.pl, NoExtraPlan{}, plan_max_radix(a.pl) <= 12, L_);
 #undef L_
-    }
 }
 
 void launch_vz_passB(const VzArgsB& a, cudaStream_t s) {

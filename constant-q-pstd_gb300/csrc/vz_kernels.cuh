@@ -602,9 +602,12 @@ __global__ void __maxnreg__(QP_WIDE_REGS) lr_xconv_kernel(LrxArgs a) {
 }
 
 // z pass of the low-rank pressure term: psc (+)= sum_b c_b(x) q_b(x) over the
-// factors b0 .. b0+nb-1 (nb <= 3), q_b the inverse z transform of half spectrum
-// b; the first launch (b0 = 0) overwrites psc.  The factors are written out in
-// sequence like z pass B's terms: a loop around the transform spills registers.
+// factors b0 .. b0+nb-1 (nb <= lr_terms<FP>()), q_b the inverse z transform of
+// half spectrum b; the first launch (b0 = 0) overwrites psc.  The factors are
+// written out in sequence like z pass B's terms: a loop around the transform
+// spills registers.  The run-time-plan instances take one factor per launch
+// (three copies of their radix switch spilled 3 KB).
+template <class FP> constexpr int lr_terms() { return FP::kCompiled ? 3 : 1; }
 template <class FP>
 __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) lr_zsum_kernel(LrsArgs a, int b0, int nb) {
     ZPASS_SETUP
@@ -623,8 +626,8 @@ __global__ void __maxnreg__(FP::kMaxRadix <= 12 ? QP_R12_REGS : QP_PASS_REGS) lr
         __syncthreads();
     };
     term(b0, true);
-    if (nb > 1) term(b0 + 1, false);
-    if (nb > 2) term(b0 + 2, false);
+    if (lr_terms<FP>() > 1 && nb > 1) term(b0 + 1, false);
+    if (lr_terms<FP>() > 2 && nb > 2) term(b0 + 2, false);
     for (int k = threadIdx.x; k < nzz; k += blockDim.x) {
         const float2 t = acc[k];
         if (has0) a.psc[r0 + k] = b0 ? a.psc[r0 + k] + t.x : t.x;
