@@ -172,7 +172,11 @@ int qpstd_batch_size(const qpstd_batch *b);
 /* The i-th shot (for qpstd_shot_set_obs / get_image / get_state ...). */
 qpstd_shot *qpstd_batch_shot(qpstd_batch *b, int i);
 int qpstd_batch_sync(qpstd_batch *b);
-/* RTM of every shot; advances are enqueued `slice` steps at a time per shot. */
+/* RTM of every shot; advances are enqueued `slice` steps at a time per shot.
+ * First moves each shot to a new stream whose CUDA priority grows with the
+ * shot's work (widest windows first), after the work already on its stream:
+ * a stream taken from qpstd_shot_stream before this call is not the shot's
+ * stream afterwards. */
 int qpstd_batch_rtm_device(qpstd_batch *b, int slice);
 int qpstd_batch_pipeline_begin(qpstd_batch *b);
 int qpstd_batch_pipeline_step(qpstd_batch *b, int t, int last);
