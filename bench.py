@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 Constant-Q-PSTD time-stepping path.
 
-Prints one JSON line.  Default workload: config 4, batched Q-RTM (64 shots with
+Prints one JSON line.  Default workload: batched Q-RTM (64 shots with
 uneven windows nx ~ U(600, 2000) cut from a 600 x 6000 parent model, nz = 600,
 CPML 30, dt = 0.5 ms, nt = 5000, 30 revolve snapshots).  A timed "step" is one
 time step of every shot of the batch (the fused PSTD pipeline, all shots'
@@ -9,13 +9,13 @@ kernels in flight on their own streams, inputs resident in HBM; the working
 set is far larger than L2).  `e2e` runs whole Q-RTM shots (revolve recompute
 included) through the C ABI with host buffers, host<->device copies inside the
 timed region.  `cpu_baseline` times the FP64 C oracle (a CPU restatement of the
-reference's update equations) on the machine's host cores.
+reference's update equations) on the host cores of the GPU's machine.
 
 --impl reference times the reference arm: the reference has no CPU stepping
 path (every step runs on a GPU through cuFFT), so the arm runs the oracle, the
 FP64 port of its equations, on all host cores, one step of shot 0 per bench
 step.  The reference's own cuFFT programs, built and run on the GB300 for the
-first two configurations, are timed separately (tests/golden/make_reference_gpu.py).
+aps and vaps workloads (the 439 x 200 grids), are timed separately (tests/golden/make_reference_gpu.py).
 """
 from __future__ import annotations
 
@@ -248,7 +248,7 @@ def run_reference(args, ws, rank):
 
 
 def serve_requests(n: int, seed: int, nt_scale: float):
-    """Config 5 request stream: kinds 40/30/20/10 % aps/vaps/artm/qrtm, model
+    """The serving request stream: kinds 40/30/20/10 % aps/vaps/artm/qrtm, model
     grids log-uniform from 256 x 256 to 2048 (z) x 4096 (x), nt ~ U(2000, 8000)
     (times nt_scale), CPML 20, dx = dz = 10 m, dt = 0.5 ms, 30 snapshots."""
     import qpstd
@@ -261,7 +261,7 @@ def serve_requests(n: int, seed: int, nt_scale: float):
 
 
 def run_serve(args, ws, rank):
-    """Serving mix (config 5) through qpstd_server: Poisson arrivals, latency
+    """Serving mix through qpstd_server: Poisson arrivals, latency
     p50/p99, shots/hour; the plain per-shot path serves the same stream one
     request at a time (FIFO from the measured plain service times)."""
     import torch
@@ -363,7 +363,7 @@ def main():
                     help="run only the first N shots of the workload (small cases for profiling)")
     ap.add_argument("--form", default="power", choices=["power", "lowrank"],
                     help="constant-Q workloads: the reference's executed power-expansion form, or the low-rank "
-                         "form of the pressure term (rank 5 for qrtm4, 4 for vaps2, as the configurations state)")
+                         "form of the pressure term (rank 5 for qrtm4, 4 for vaps2)")
     ap.add_argument("--requests", type=int, default=500, help="serve5: requests in the stream")
     ap.add_argument("--nt-scale", type=float, default=1.0, help="serve5: scale of the nt draws")
     ap.add_argument("--load", type=float, default=1.0, help="serve5: offered load (x a 3 Gpts/s server)")

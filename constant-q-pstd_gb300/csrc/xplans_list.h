@@ -8,7 +8,7 @@
 // the radices in the order the planner factors that length (odd radices first),
 // so a compiled plan and the planner's plan for its length are the same passes.
 // The lengths cover the windows of the batched Q-RTM workload (1319 <= m <=
-// 4096) at steps of 7-15 %, the 439-wide window of the small configurations
+// 4096) at steps of 7-15 %, the 439-wide window of the 160 x 398 model
 // (900) and the 2461-wide one of the large RTM (5040).  Three groups, one
 // translation unit each (xplans_g0.cu ..), keep the build parallel.
 #pragma once

@@ -8,7 +8,7 @@ programs (sgpstd-qmodeling: the aps and vaps mains, acps4.cu, acsglw.cu,
 funca.c, func.c, src.c and their headers) to baseline/_ref/src, which git
 ignores and which travels with the working tree.  It writes one more pair of
 files there: the two mains with `#define pml 10` changed to 20 (the CPML width
-the benchmark configurations ask for).  oracle/refgpu/Makefile builds them.
+of the aps and vaps workloads).  oracle/refgpu/Makefile builds them.
 
     python oracle/refgpu/stage.py [reference tree]   # default: $QPSTD_REFERENCE,
                                                       # else ../reference beside the repo

@@ -14,8 +14,8 @@ sm_103a with a one-rank MPI stub) and runs, in project trees laid out as the
 reference expects (tests/refgpu_case.py):
   * pins: aps (400 steps) and vaps (300 steps) as shipped (CPML 10) on the
     seeded one-shot case; their reca / recva gathers go to OUTDIR/reference_gpu_gathers.npz;
-  * timing: aps and vaps with the CPML patched to 20 on the same shot (the
-    first two benchmark configurations: 2000 and 3000 steps), each also at 200
+  * timing: aps and vaps with the CPML patched to 20 on the same shot (the aps
+    and vaps workloads: 2000 and 3000 steps), each also at 200
     steps so the per-step time excludes start-up; OUTDIR/reference_gpu_timing.json.
 Everything the reference programs do (cuFFT plans, a host copy of p and a
 stream synchronisation every step) is inside the wall times.

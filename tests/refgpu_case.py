@@ -1,6 +1,6 @@
 """The shot on which the reference's own cuFFT programs pin the oracle.
 
-TEST INFRASTRUCTURE.  One shot of the first benchmark configuration's geometry:
+TEST INFRASTRUCTURE.  One shot of the 160 x 398 model geometry:
 a seeded 398 (x) x 160 (z) layered model (5 layers, one anomaly, Gardner
 density, Q per layer in 20..200), dx = dz = 10 m, the source at x = 1990 m,
 z = 20 m, 398 receivers at z = 20 m from x = 0 to 3970 m, a 20 Hz Ricker

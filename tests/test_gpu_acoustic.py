@@ -8,7 +8,7 @@ import pytest
 
 import oracle as O
 import qpstd
-from cases import cfg1_shot, rel_l2, small_shot
+from cases import grid439_shot, rel_l2, small_shot
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-4
@@ -45,9 +45,9 @@ def test_aps_small_shot_gather():
         assert rel_l2(st[f], ref_st[f]) < TOL, f
 
 
-def test_aps_config1_grid_gather():
-    """Config 1 padded grid (439 prime x 200), shortened to 400 steps."""
-    d = cfg1_shot(qpstd.APS, nt=400)
+def test_aps_439x200_grid_gather():
+    """The 439 prime x 200 padded grid of the 160 x 398 model, shortened to 400 steps."""
+    d = grid439_shot(qpstd.APS, nt=400)
     ref_g = O.OracleShot(d).model()
     g = qpstd.model_shot(d)
     assert g.shape == (400, 398)

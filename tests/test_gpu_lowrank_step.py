@@ -13,7 +13,7 @@ import pytest
 
 import oracle as O
 import qpstd
-from cases import cfg1_shot, rel_l2, small_shot
+from cases import grid439_shot, rel_l2, small_shot
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-4
@@ -48,9 +48,9 @@ def test_lowrank_steps_from_random_state(nx, nz, rank):
     assert rel_l2(g, ref_g) < TOL
 
 
-def test_lowrank_config2_grid_gather():
-    """The second configuration's grid (439 x 200) at rank 4, shortened to 200 steps."""
-    d = cfg1_shot(qpstd.VAPS, nt=200)
+def test_lowrank_439x200_grid_gather():
+    """The 439 x 200 padded grid of the 160 x 398 model at rank 4, shortened to 200 steps."""
+    d = grid439_shot(qpstd.VAPS, nt=200)
     f = _factors(d, 4)
     ref_g = O.OracleShot(dict(d, lowrank=f)).model()
     sh = qpstd.Shot(d)

@@ -7,7 +7,7 @@ import pytest
 
 import oracle as O
 import qpstd
-from cases import cfg1_shot, rel_l2, small_shot
+from cases import grid439_shot, rel_l2, small_shot
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-4
@@ -43,9 +43,9 @@ def test_vaps_small_shot_gather():
         assert rel_l2(st[f], ref_st[f]) < TOL, f
 
 
-def test_vaps_config1_grid_gather():
-    """Config 2 geometry (439 prime x 200 padded grid), shortened to 300 steps."""
-    d = cfg1_shot(qpstd.VAPS, nt=300)
+def test_vaps_439x200_grid_gather():
+    """The 160 x 398 model geometry (439 prime x 200 padded grid), shortened to 300 steps."""
+    d = grid439_shot(qpstd.VAPS, nt=300)
     ref_g = O.OracleShot(d).model()
     g = qpstd.model_shot(d)
     assert rel_l2(g, ref_g) < TOL
